@@ -1,0 +1,226 @@
+"""Python mirror of the reference's call surface, over the C ABI.
+
+Two levels, as in the reference's ecosystem:
+
+* ``execute(kernel_name, params, global_range)`` -- the drop-in for one .cl
+  kernel launch: the kernel's name and its named parameters (``src``/``dst``
+  images, ``dim``/``N``/``s``/``Nx``/``Ny``/``Nz`` scalars), bound by name.
+  This is how CLIc / clij-clearcl enqueue e.g. ``gaussian_blur_separable_3d``
+  (kernels/gaussian_blur_separable_3d_x.cl:6-12).
+* Orchestrator functions in pyclesperanto's vocabulary (``gaussian_blur``,
+  ``mean_box``, ``minimum_box``, ``maximum_box``, ``median_box``,
+  ``median_sphere``, ``erode_box`` ... ``sobel``) that pick the kernel, the
+  per-axis N and run the separable passes.
+
+Images are CUDA tensors (torch is only the device-memory container here),
+C-contiguous, shape (depth, height, width) or (height, width): x fastest,
+exactly the reference's buffer layout.  Pixel types: uint8, int8, uint16,
+int16, float32.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Mapping
+
+import torch
+
+from . import _lib as L
+
+_DT = {torch.uint8: L.U8, torch.int8: L.I8, torch.uint16: L.U16, torch.int16: L.I16, torch.float32: L.F32}
+_TORCH = {v: k for k, v in _DT.items()}
+
+
+def dtype_code(dt: torch.dtype) -> int:
+    try:
+        return _DT[dt]
+    except KeyError:
+        raise L.ClkError(L.UNSUPPORTED_DTYPE, f"pixel type {dt} is not one of {list(_DT)}") from None
+
+
+def torch_dtype(code: int) -> torch.dtype:
+    return _TORCH[code]
+
+
+def image_of(t: torch.Tensor) -> L.clk_image:
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise L.ClkError(L.BAD_ARG, "images must be CUDA tensors")
+    if not t.is_contiguous():
+        raise L.ClkError(L.BAD_ARG, "images must be C-contiguous (x fastest)")
+    if t.dim() == 2:
+        return L.clk_image(t.data_ptr(), dtype_code(t.dtype), 2, t.shape[1], t.shape[0], 1)
+    if t.dim() == 3:
+        return L.clk_image(t.data_ptr(), dtype_code(t.dtype), 3, t.shape[2], t.shape[1], t.shape[0])
+    raise L.ClkError(L.BAD_ARG, f"images are 2-D or 3-D, got shape {tuple(t.shape)}")
+
+
+def _defines(defines: Mapping[str, object] | None):
+    if not defines:
+        return None, 0, []
+    keep = [(str(k).encode(), str(v).encode()) for k, v in defines.items()]
+    arr = (L.clk_define * len(keep))(*[L.clk_define(k, v) for k, v in keep])
+    return arr, len(keep), keep
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, torch.cuda.Stream):
+        return stream.cuda_stream
+    return int(stream)
+
+
+def execute(kernel_name: str, params: Mapping[str, object], global_range=None,
+            defines: Mapping[str, object] | None = None, stream=None) -> None:
+    """Launch one reference kernel by name with named parameters.
+
+    params maps parameter names to CUDA tensors (images), ints or floats.
+    global_range: (x, y[, z]) work size; default the dst extent.
+    """
+    lib = L.load()
+    args, keep = [], []
+    for name, v in params.items():
+        nb = name.encode()
+        keep.append(nb)
+        if isinstance(v, torch.Tensor):
+            args.append(L.clk_arg(nb, L.ARG_IMAGE, 0, 0.0, image_of(v)))
+        elif isinstance(v, bool) or not isinstance(v, (int, float)):
+            raise L.ClkError(L.BAD_ARG, f"parameter {name!r}: unsupported value {v!r}")
+        elif isinstance(v, int):
+            args.append(L.clk_arg(nb, L.ARG_INT, int(v), 0.0, L.clk_image()))
+        else:
+            args.append(L.clk_arg(nb, L.ARG_FLOAT, 0, float(v), L.clk_image()))
+    arr = (L.clk_arg * len(args))(*args)
+    g = None
+    if global_range is not None:
+        gr = list(global_range) + [1] * (3 - len(global_range))
+        g = (C.c_size_t * 3)(*gr)
+    darr, nd, _k = _defines(defines)
+    L.check(lib.clk_execute(kernel_name.encode(), arr, len(args), g, darr, nd, _stream(stream)))
+
+
+def separable(kernel_name: str, src: torch.Tensor, dst: torch.Tensor, N, s=(0.0, 0.0, 0.0),
+              defines: Mapping[str, object] | None = None, stream=None) -> torch.Tensor:
+    """The whole X->Y(->Z) separable filter (the orchestrator's driver)."""
+    lib = L.load()
+    n = list(N) + [1] * (3 - len(N))
+    sg = [float(v) for v in s] + [0.0] * (3 - len(s))
+    di, si = image_of(dst), image_of(src)
+    darr, nd, _k = _defines(defines)
+    L.check(lib.clk_separable(kernel_name.encode(), C.byref(di), C.byref(si), (C.c_int32 * 3)(*n),
+                              (C.c_float * 3)(*sg), darr, nd, _stream(stream)))
+    return dst
+
+
+def supported(kernel_name: str, src_dtype: torch.dtype, dst_dtype: torch.dtype, ndim: int) -> bool:
+    return bool(L.load().clk_supported(kernel_name.encode(), dtype_code(src_dtype), dtype_code(dst_dtype), ndim))
+
+
+def kernel_names() -> list[str]:
+    lib = L.load()
+    return [lib.clk_kernel_name(i).decode() for i in range(lib.clk_kernel_count())]
+
+
+def version() -> str:
+    return L.load().clk_version().decode()
+
+
+def launch_count() -> int:
+    return int(L.load().clk_launch_count())
+
+
+# ----------------------------------------------------------------- orchestrator
+
+def sigma_to_n(sigma: float) -> int:
+    """Window N of a Gaussian of standard deviation sigma: radius ceil(3 sigma)."""
+    return 2 * int(math.ceil(3.0 * float(sigma))) + 1 if sigma > 0 else 1
+
+
+def _out(src: torch.Tensor, dst, dtype=None) -> torch.Tensor:
+    if dst is not None:
+        return dst
+    return torch.empty_like(src, dtype=dtype or src.dtype)
+
+
+def _suffix(t: torch.Tensor) -> str:
+    return "_2d" if t.dim() == 2 else "_3d"
+
+
+def gaussian_blur(src, dst=None, sigma_x=0.0, sigma_y=0.0, sigma_z=0.0, stream=None, defines=None):
+    dst = _out(src, dst, torch.float32)
+    sig = (sigma_x, sigma_y, sigma_z)
+    return separable("gaussian_blur_separable" + _suffix(src), src, dst, [sigma_to_n(v) for v in sig], sig,
+                     defines, stream)
+
+
+def _box(kernel, src, dst, rx, ry, rz, stream, defines):
+    dst = _out(src, dst)
+    r = (rx, ry, rz)
+    return separable(kernel + _suffix(src), src, dst, [2 * int(v) + 1 for v in r], [float(v) for v in r],
+                     defines, stream)
+
+
+def mean_box(src, dst=None, radius_x=1, radius_y=1, radius_z=1, stream=None, defines=None):
+    return _box("mean_separable", src, dst, radius_x, radius_y, radius_z, stream, defines)
+
+
+def minimum_box(src, dst=None, radius_x=1, radius_y=1, radius_z=1, stream=None, defines=None):
+    return _box("minimum_separable", src, dst, radius_x, radius_y, radius_z, stream, defines)
+
+
+def maximum_box(src, dst=None, radius_x=1, radius_y=1, radius_z=1, stream=None, defines=None):
+    return _box("maximum_separable", src, dst, radius_x, radius_y, radius_z, stream, defines)
+
+
+def _median(kind, src, dst, rx, ry, rz, stream, defines):
+    dst = _out(src, dst)
+    p = {"dst": dst, "src": src, "Nx": 2 * int(rx) + 1, "Ny": 2 * int(ry) + 1}
+    if src.dim() == 3:
+        p["Nz"] = 2 * int(rz) + 1
+    execute(kind + _suffix(src), p, defines=defines, stream=stream)
+    return dst
+
+
+def median_box(src, dst=None, radius_x=1, radius_y=1, radius_z=1, stream=None, defines=None):
+    return _median("median_box", src, dst, radius_x, radius_y, radius_z, stream, defines)
+
+
+def median_sphere(src, dst=None, radius_x=1, radius_y=1, radius_z=1, stream=None, defines=None):
+    return _median("median_sphere", src, dst, radius_x, radius_y, radius_z, stream, defines)
+
+
+def _morph(kind, src, dst, radius, stream, defines):
+    """r=1 is one launch of the reference kernel; radius r>1 applies it r
+    times (the kernels have no radius parameter, erode_sphere_3d_x.cl:3-6)."""
+    dst = _out(src, dst)
+    if radius < 1:
+        dst.copy_(src.to(dst.dtype))
+        return dst
+    cur = src
+    for i in range(int(radius)):
+        out = dst if i == radius - 1 else torch.empty_like(dst)
+        execute(kind + _suffix(src), {"src": cur, "dst": out}, defines=defines, stream=stream)
+        cur = out
+    return dst
+
+
+def erode_box(src, dst=None, radius=1, stream=None, defines=None):
+    return _morph("erode_box", src, dst, radius, stream, defines)
+
+
+def erode_sphere(src, dst=None, radius=1, stream=None, defines=None):
+    return _morph("erode_sphere", src, dst, radius, stream, defines)
+
+
+def dilate_box(src, dst=None, radius=1, stream=None, defines=None):
+    return _morph("dilate_box", src, dst, radius, stream, defines)
+
+
+def dilate_sphere(src, dst=None, radius=1, stream=None, defines=None):
+    return _morph("dilate_sphere", src, dst, radius, stream, defines)
+
+
+def sobel(src, dst=None, stream=None, defines=None):
+    dst = _out(src, dst, torch.float32)
+    execute("sobel" + _suffix(src), {"dst": dst, "src": src}, defines=defines, stream=stream)
+    return dst

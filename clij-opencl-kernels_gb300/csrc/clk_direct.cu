@@ -1,0 +1,307 @@
+// clk_direct.cu - generic kernels: one thread per output voxel, every
+// pixel-type pair, float arithmetic in the reference's own order with
+// explicitly rounded operations (__fmul_rn / __fadd_rn never contract into
+// FMA), so their results are bit-identical to the reference's.  They back
+// clk_execute's single-pass drop-in and every case the fused fast paths do
+// not cover.
+#include "clk_common.cuh"
+
+namespace clk {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ void decode(int64_t i, const Range& r, int& x, int& y, int& z) {
+  const int64_t xy = (int64_t)r.x * r.y;
+  z = (int)(i / xy);
+  const int64_t rem = i - (int64_t)z * xy;
+  y = (int)(rem / r.x);
+  x = (int)(rem - (int64_t)y * r.x);
+}
+
+inline unsigned grid_for(int64_t n) {
+  const int64_t g = (n + kBlock - 1) / kBlock;
+  return (unsigned)(g < 152 * 64 ? (g < 1 ? 1 : g) : 152 * 64);
+}
+
+// One separable pass (gaussian_blur_separable_3d_x.cl:14-34,
+// mean_separable_3d_x.cl:12-29, minimum/maximum_separable_3d_x.cl:12-23).
+template <class S, class D, int OP>
+__global__ void __launch_bounds__(kBlock)
+    k_sep_pass(D* __restrict__ dst, const S* __restrict__ src, Dims3 sd, Dims3 dd, Range r, int dim,
+               const __grid_constant__ SepTaps taps, bool rte) {
+  const int dx = dim == 0, dy = dim == 1, dz = dim == 2;
+  const int c = taps.c;
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    float res;
+    if constexpr (OP == SEP_GAUSS) {
+      res = 0.f;
+      for (int v = -c; v <= c; ++v)
+        res = __fadd_rn(res, __fmul_rn(taps.h[v + c], ldf(src, atc(sd, x + v * dx, y + v * dy, z + v * dz))));
+      res = __fdiv_rn(res, taps.hsum);
+    } else if constexpr (OP == SEP_MEAN) {
+      res = 0.f;
+      for (int v = -c; v <= c; ++v) res = __fadd_rn(res, ldf(src, atc(sd, x + v * dx, y + v * dy, z + v * dz)));
+      res = __fdiv_rn(res, c >= 0 ? (float)(2 * c + 1) : 0.f);
+    } else {
+      res = ldf(src, atc(sd, x, y, z));
+      for (int v = -c; v <= c; ++v) {
+        const float t = ldf(src, atc(sd, x + v * dx, y + v * dy, z + v * dz));
+        if constexpr (OP == SEP_MIN) res = t < res ? t : res;
+        else res = res < t ? t : res;
+      }
+    }
+    dst[at(dd, x, y, z)] = convert_sat<D>(res, rte);
+  }
+}
+
+// copy_3d_x.cl:13-14: float through, then CONVERT.
+template <class S, class D>
+__global__ void __launch_bounds__(kBlock)
+    k_copy(D* __restrict__ dst, const S* __restrict__ src, Dims3 sd, Dims3 dd, Range r, bool rte) {
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    dst[at(dd, x, y, z)] = convert_sat<D>(ldf(src, atc(sd, x, y, z)), rte);
+  }
+}
+
+// median_box/sphere (median_box_3d_x.cl:3-20,41-64): gather, stable
+// insertion sort, element n/2.
+template <class T, int CAP>
+__global__ void __launch_bounds__(kBlock)
+    k_median(T* __restrict__ dst, const T* __restrict__ src, Dims3 sd, Dims3 dd, Range r,
+             const __grid_constant__ MedianNbhd m) {
+  T a[CAP];
+  const int n = m.n;
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    for (int k = 0; k < n; ++k) {
+      const char4 o = m.off[k];
+      a[k] = __ldg(src + atc(sd, x + o.x, y + o.y, z + o.z));
+    }
+    for (int k = 1; k < n; ++k) {
+      const T t = a[k];
+      int j = k - 1;
+      while (j >= 0 && t < a[j]) {
+        a[j + 1] = a[j];
+        --j;
+      }
+      a[j + 1] = t;
+    }
+    dst[at(dd, x, y, z)] = a[n / 2];
+  }
+}
+
+// erode/dilate box/sphere (erode_box_3d_x.cl:14-37, erode_sphere_3d_x.cl:
+// 14-37, dilate_box_3d_x.cl:14-37, dilate_sphere_3d_x.cl:14-38 and the _2d
+// files), replaying the early-exit read order so the written value,
+// including the sign of a float zero, is the one the kernel writes.
+template <class S, class D, bool ERODE, bool SPHERE, bool THREE>
+__global__ void __launch_bounds__(kBlock)
+    k_morph(D* __restrict__ dst, const S* __restrict__ src, Dims3 sd, Dims3 dd, Range r, bool rte) {
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    float value = ldf(src, atc(sd, x, y, z));
+    const bool go = ERODE ? (value != 0.f) : ((THREE && !SPHERE) ? (value < 1.f) : (value == 0.f));
+    if (go) {
+      if constexpr (SPHERE) {
+        const int fx[6] = {1, -1, 0, 0, 0, 0}, fy[6] = {0, 0, 1, -1, 0, 0}, fz[6] = {0, 0, 0, 0, 1, -1};
+#pragma unroll
+        for (int k = 0; k < (THREE ? 6 : 4); ++k) {
+          value = ldf(src, atc(sd, x + fx[k], y + fy[k], z + fz[k]));
+          if (ERODE ? (value == 0.f) : (value != 0.f)) break;
+        }
+      } else {
+        constexpr int zr = THREE ? 1 : 0;
+        bool stop = false;
+        for (int ax = -1; ax <= 1 && !stop; ++ax)
+          for (int ay = -1; ay <= 1 && !stop; ++ay)
+            for (int az = -zr; az <= zr && !stop; ++az) {
+              value = ldf(src, atc(sd, x + ax, y + ay, z + az));
+              stop = ERODE ? (value == 0.f) : (value != 0.f);
+            }
+      }
+    }
+    if (value != 0.f) value = 1.f;
+    dst[at(dd, x, y, z)] = convert_sat<D>(value, rte);
+  }
+}
+
+// sobel_2d_x.cl:14-41: the weighted sums are double-promoted (double
+// literals) and stored to float.
+template <class S, class D>
+__global__ void __launch_bounds__(kBlock)
+    k_sobel2d(D* __restrict__ dst, const S* __restrict__ src, Dims3 sd, Dims3 dd, Range r, bool rte) {
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    auto v = [&](int ddx, int ddy) -> double { return (double)ldf(src, atc(sd, x + ddx, y + ddy, 0)); };
+    const double tl = v(-1, -1), tr = v(1, -1), bl = v(-1, 1), br = v(1, 1);
+    const double l = v(-1, 0), rr = v(1, 0), t = v(0, -1), b = v(0, 1);
+    double ax = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(-tl, l * -2.0), -bl), tr), rr * 2.0), br);
+    double ay = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(-tl, t * -2.0), -tr), bl), b * 2.0), br);
+    const float rx = __double2float_rn(ax), ry = __double2float_rn(ay);
+    const float res = __fsqrt_rn(__fadd_rn(__fmul_rn(rx, rx), __fmul_rn(ry, ry)));
+    dst[at(dd, x, y, z)] = convert_sat<D>(res, rte);
+  }
+}
+
+// Coefficient of tap (m, n, k), k = 0..3, of the 3x3x4 window of
+// sobel_3d_x.cl:44-52 for component comp: the arrays of :33-41 read through
+// their flat layout, the one element past the array pinned to 0.
+__host__ __device__ constexpr int sobel3d_coef(int comp, int m, int n, int k) {
+  const int flat = 9 * m + 3 * n + k;
+  if (flat >= 27) return 0;
+  const int mm = flat / 9, nn = (flat / 3) % 3, kk = flat % 3;
+  const int h0 = mm == 1 ? 2 : 1, h1 = nn == 1 ? 2 : 1, h2 = kk == 1 ? 2 : 1;
+  const int p0 = 1 - mm, p1 = 1 - nn, p2 = 1 - kk;  // hp = {1, 0, -1}
+  return comp == 0 ? p0 * h1 * h2 : (comp == 1 ? h0 * p1 * h2 : h0 * h1 * p2);
+}
+
+// sobel_3d_x.cl:43-56, sums in the kernel's order.  A term's type follows C:
+// int * uint is uint (negative coefficients wrap), int * int is int,
+// int * float is float; each term is added to a float sum.
+template <class S, class D>
+__global__ void __launch_bounds__(kBlock)
+    k_sobel3d(D* __restrict__ dst, const S* __restrict__ src, Dims3 sd, Dims3 dd, Range r, bool narrow, bool rte) {
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    float sum[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+#pragma unroll
+      for (int n = 0; n < 3; ++n)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const S raw = __ldg(src + atc(sd, x + m - 1, y + n - 1, z + k - 1));
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const int co = sobel3d_coef(c, m, n, k);
+            float term;
+            if constexpr (sizeof(S) == 4) {
+              term = __fmul_rn((float)co, raw);
+            } else if constexpr (S(-1) > S(0)) {  // unsigned pixel type
+              term = narrow ? __int2float_rn(co * (int)raw) : __uint2float_rn((uint32_t)co * (uint32_t)raw);
+            } else {
+              term = __int2float_rn(co * (int)raw);
+            }
+            sum[c] = __fadd_rn(sum[c], term);
+          }
+        }
+    const float res = __fsqrt_rn(
+        __fadd_rn(__fadd_rn(__fmul_rn(sum[0], sum[0]), __fmul_rn(sum[1], sum[1])), __fmul_rn(sum[2], sum[2])));
+    dst[at(dd, x, y, z)] = convert_sat<D>(res, rte);
+  }
+}
+
+inline Dims3 dims(const Image& im) { return Dims3{im.w, im.h, im.d}; }
+
+}  // namespace
+
+clk_status direct_sep_pass(SepOp op, const Image& dst, const Image& src, int dim, const SepTaps& taps, Range r,
+                           const Policy& p, cudaStream_t st) {
+  if (r.count() == 0) return CLK_OK;
+  const unsigned g = grid_for(r.count());
+  const bool ok = dispatch_types(src.dt, dst.dt, [&](auto s, auto d) {
+    using S = decltype(s);
+    using D = decltype(d);
+    auto* o = (D*)dst.ptr;
+    auto* in = (const S*)src.ptr;
+    switch (op) {
+      case SEP_GAUSS: k_sep_pass<S, D, SEP_GAUSS><<<g, kBlock, 0, st>>>(o, in, dims(src), dims(dst), r, dim, taps, p.rte); break;
+      case SEP_MEAN: k_sep_pass<S, D, SEP_MEAN><<<g, kBlock, 0, st>>>(o, in, dims(src), dims(dst), r, dim, taps, p.rte); break;
+      case SEP_MIN: k_sep_pass<S, D, SEP_MIN><<<g, kBlock, 0, st>>>(o, in, dims(src), dims(dst), r, dim, taps, p.rte); break;
+      case SEP_MAX: k_sep_pass<S, D, SEP_MAX><<<g, kBlock, 0, st>>>(o, in, dims(src), dims(dst), r, dim, taps, p.rte); break;
+    }
+  });
+  if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "separable pass: pixel types %d -> %d", src.dt, dst.dt);
+  count_launch();
+  return check_launch("separable pass");
+}
+
+clk_status direct_copy(const Image& dst, const Image& src, Range r, const Policy& p, cudaStream_t st) {
+  if (r.count() == 0) return CLK_OK;
+  const bool ok = dispatch_types(src.dt, dst.dt, [&](auto s, auto d) {
+    using S = decltype(s);
+    using D = decltype(d);
+    k_copy<S, D><<<grid_for(r.count()), kBlock, 0, st>>>((D*)dst.ptr, (const S*)src.ptr, dims(src), dims(dst), r,
+                                                         p.rte);
+  });
+  if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "copy: pixel types %d -> %d", src.dt, dst.dt);
+  count_launch();
+  return check_launch("copy");
+}
+
+clk_status direct_median(const Image& dst, const Image& src, const MedianNbhd& m, Range r, cudaStream_t st) {
+  if (r.count() == 0) return CLK_OK;
+  if (src.dt != dst.dt)
+    return fail(CLK_UNSUPPORTED_DTYPE, "median: src and dst pixel types must match (the kernel's dst-typed array "
+                                       "makes other pairs implementation-defined)");
+  const unsigned g = grid_for(r.count());
+  const bool ok = dispatch_type(src.dt, [&](auto t) {
+    using T = decltype(t);
+    if (m.n <= 32)
+      k_median<T, 32><<<g, kBlock, 0, st>>>((T*)dst.ptr, (const T*)src.ptr, dims(src), dims(dst), r, m);
+    else if (m.n <= 128)
+      k_median<T, 128><<<g, kBlock, 0, st>>>((T*)dst.ptr, (const T*)src.ptr, dims(src), dims(dst), r, m);
+    else
+      k_median<T, kMaxMedian><<<g, kBlock, 0, st>>>((T*)dst.ptr, (const T*)src.ptr, dims(src), dims(dst), r, m);
+  });
+  if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "median: pixel type %d", src.dt);
+  count_launch();
+  return check_launch("median");
+}
+
+clk_status direct_morph(bool erode, bool sphere, const Image& dst, const Image& src, Range r, const Policy& p,
+                        cudaStream_t st) {
+  if (r.count() == 0) return CLK_OK;
+  const unsigned g = grid_for(r.count());
+  const bool three = src.ndim == 3;
+  const bool ok = dispatch_types(src.dt, dst.dt, [&](auto s, auto d) {
+    using S = decltype(s);
+    using D = decltype(d);
+    auto* o = (D*)dst.ptr;
+    auto* in = (const S*)src.ptr;
+    const Dims3 a = dims(src), b = dims(dst);
+    const int sel = (erode ? 4 : 0) | (sphere ? 2 : 0) | (three ? 1 : 0);
+    switch (sel) {
+      case 0: k_morph<S, D, false, false, false><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case 1: k_morph<S, D, false, false, true><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case 2: k_morph<S, D, false, true, false><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case 3: k_morph<S, D, false, true, true><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case 4: k_morph<S, D, true, false, false><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case 5: k_morph<S, D, true, false, true><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case 6: k_morph<S, D, true, true, false><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case 7: k_morph<S, D, true, true, true><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+    }
+  });
+  if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "morphology: pixel types %d -> %d", src.dt, dst.dt);
+  count_launch();
+  return check_launch("morphology");
+}
+
+clk_status direct_sobel(const Image& dst, const Image& src, Range r, const Policy& p, cudaStream_t st) {
+  if (r.count() == 0) return CLK_OK;
+  const unsigned g = grid_for(r.count());
+  const bool ok = dispatch_types(src.dt, dst.dt, [&](auto s, auto d) {
+    using S = decltype(s);
+    using D = decltype(d);
+    if (src.ndim == 2)
+      k_sobel2d<S, D><<<g, kBlock, 0, st>>>((D*)dst.ptr, (const S*)src.ptr, dims(src), dims(dst), r, p.rte);
+    else
+      k_sobel3d<S, D><<<g, kBlock, 0, st>>>((D*)dst.ptr, (const S*)src.ptr, dims(src), dims(dst), r,
+                                            p.sobel_narrow, p.rte);
+  });
+  if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "sobel: pixel types %d -> %d", src.dt, dst.dt);
+  count_launch();
+  return check_launch("sobel");
+}
+
+}  // namespace clk

@@ -1,0 +1,92 @@
+// clk_internal.h - host-side interface between the C-ABI dispatcher
+// (clk_api.cpp) and the CUDA launchers (*.cu).  Not installed.
+#pragma once
+#include <cuda_runtime_api.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "clk.h"
+
+#ifdef __CUDACC__
+#define CLK_HD __host__ __device__
+#else
+#define CLK_HD
+#endif
+
+namespace clk {
+
+constexpr int kMaxTaps = 1001;        // separable window 2c+1 (kernel params)
+constexpr int kMaxMedian = 1000;      // median neighbourhood size (kernel params)
+constexpr int kDefaultMaxArray = 1024;
+
+struct Image {
+  void* ptr;
+  int dt;    // clk_dtype
+  int ndim;  // 2 or 3
+  int w, h, d;
+  CLK_HD int64_t count() const { return (int64_t)w * h * d; }
+};
+
+struct Range {
+  int x, y, z;
+  CLK_HD int64_t count() const { return (int64_t)x * y * z; }
+};
+
+// Host-side policies the reference leaves to its preamble / host (each one
+// is a define of clk_execute, include/clk.h).
+struct Policy {
+  bool rte = false;           // CONVERT rounding half-to-even instead of toward zero
+  bool sobel_narrow = false;  // sobel_3d reads unsigned pixels as int, not uint
+  bool exact_order = false;   // reference-order float sums for float outputs too
+  int max_array = kDefaultMaxArray;
+};
+
+enum SepOp { SEP_GAUSS = 0, SEP_MEAN = 1, SEP_MIN = 2, SEP_MAX = 3 };
+
+// Taps of one separable pass: the window is v = -c..c (c = (N-1)/2 with C
+// division, gaussian_blur_separable_3d_x.cl:22); for gaussian h[v+c] and
+// their sequential float sum, computed exactly as the kernel does.
+struct SepTaps {
+  int c;
+  float hsum;
+  float h[kMaxTaps];
+};
+
+// Neighbourhood of a median launch in the kernel's loop order.
+struct MedianNbhd {
+  int n;
+  int ex, ey, ez;
+  char4 off[kMaxMedian];  // (dx, dy, dz, 0)
+};
+
+// error reporting (thread-local message) and launch accounting
+clk_status fail(clk_status st, const char* fmt, ...);
+clk_status check_launch(const char* what);
+void count_launch(int n = 1);
+
+int dtype_size(int dt);
+bool gauss_taps(int N, float s, SepTaps* t);  // false: window too large
+void box_taps(int N, SepTaps* t);
+bool median_nbhd(bool sphere, int ndim, int Nx, int Ny, int Nz, MedianNbhd* m);
+
+// ---- generic ("direct") kernels: one thread per output voxel, every
+// pixel-type pair, the reference's own evaluation order (bit-exact).
+clk_status direct_sep_pass(SepOp op, const Image& dst, const Image& src, int dim, const SepTaps& taps, Range r,
+                           const Policy& p, cudaStream_t st);
+clk_status direct_copy(const Image& dst, const Image& src, Range r, const Policy& p, cudaStream_t st);
+clk_status direct_median(const Image& dst, const Image& src, const MedianNbhd& m, Range r, cudaStream_t st);
+clk_status direct_morph(bool erode, bool sphere, const Image& dst, const Image& src, Range r, const Policy& p,
+                        cudaStream_t st);
+clk_status direct_sobel(const Image& dst, const Image& src, Range r, const Policy& p, cudaStream_t st);
+
+// ---- fused / tiled fast paths.  Return CLK_UNSUPPORTED_DTYPE (without
+// setting an error) when the case is not covered, so the caller falls back.
+clk_status fused_separable(SepOp op, const Image& dst, const Image& src, const SepTaps taps[3], const bool skip[3],
+                           const Policy& p, cudaStream_t st);
+clk_status fast_morph(bool erode, bool sphere, int iterations, const Image& dst, const Image& src, const Policy& p,
+                      cudaStream_t st);
+clk_status fast_sobel(const Image& dst, const Image& src, const Policy& p, cudaStream_t st);
+clk_status fast_median(bool sphere, const Image& dst, const Image& src, const MedianNbhd& m, cudaStream_t st);
+
+}  // namespace clk
