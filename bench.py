@@ -247,12 +247,10 @@ def main():
             p = {"src": src_t, "dst": out_t}
             p.update(params)
             clk.execute(kernel, p, stream=stream)
-        else:
-            cur = src_t
-            for i in range(params):
-                o = out_t if i == params - 1 else tmp_mask
-                clk.execute(kernel, {"src": cur, "dst": o}, stream=stream)
-                cur = o
+        elif params == 1:  # r=1: one launch of the reference kernel
+            clk.execute(kernel, {"src": src_t, "dst": out_t}, stream=stream)
+        else:  # radius r: r successive launches, fused in pairs
+            clk.morphology(kernel, src_t, out_t, params, stream=stream)
 
     def step(srcs):
         for name, kind, kernel, params, srcn, ddt, bpv in spec:

@@ -44,7 +44,7 @@ class ClkError(RuntimeError):
         self.status = status
 
 
-EXPORTS = ["clk_execute", "clk_separable", "clk_supported", "clk_last_error_string", "clk_version",
+EXPORTS = ["clk_execute", "clk_separable", "clk_morphology", "clk_supported", "clk_last_error_string", "clk_version",
            "clk_kernel_count", "clk_kernel_name", "clk_launch_count"]
 
 _lib = None
@@ -64,6 +64,9 @@ def load() -> C.CDLL:
     lib.clk_separable.argtypes = [C.c_char_p, C.POINTER(clk_image), C.POINTER(clk_image), C.POINTER(C.c_int32),
                                   C.POINTER(C.c_float), C.POINTER(clk_define), C.c_size_t, C.c_void_p]
     lib.clk_separable.restype = C.c_int
+    lib.clk_morphology.argtypes = [C.c_char_p, C.POINTER(clk_image), C.POINTER(clk_image), C.c_int32,
+                                   C.POINTER(clk_define), C.c_size_t, C.c_void_p]
+    lib.clk_morphology.restype = C.c_int
     lib.clk_supported.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32]
     lib.clk_supported.restype = C.c_int
     lib.clk_last_error_string.restype = C.c_char_p

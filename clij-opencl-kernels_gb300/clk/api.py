@@ -189,19 +189,23 @@ def median_sphere(src, dst=None, radius_x=1, radius_y=1, radius_z=1, stream=None
     return _median("median_sphere", src, dst, radius_x, radius_y, radius_z, stream, defines)
 
 
-def _morph(kind, src, dst, radius, stream, defines):
-    """r=1 is one launch of the reference kernel; radius r>1 applies it r
-    times (the kernels have no radius parameter, erode_sphere_3d_x.cl:3-6)."""
-    dst = _out(src, dst)
-    if radius < 1:
-        dst.copy_(src.to(dst.dtype))
-        return dst
-    cur = src
-    for i in range(int(radius)):
-        out = dst if i == radius - 1 else torch.empty_like(dst)
-        execute(kind + _suffix(src), {"src": cur, "dst": out}, defines=defines, stream=stream)
-        cur = out
+def morphology(kernel_name: str, src: torch.Tensor, dst: torch.Tensor, iterations: int = 1,
+               defines: Mapping[str, object] | None = None, stream=None) -> torch.Tensor:
+    """`iterations` successive launches of an r=1 erode/dilate kernel (the
+    kernels have no radius parameter, erode_sphere_3d_x.cl:3-6); byte images
+    run two iterations fused per pass."""
+    lib = L.load()
+    di, si = image_of(dst), image_of(src)
+    darr, nd, _k = _defines(defines)
+    L.check(lib.clk_morphology(kernel_name.encode(), C.byref(di), C.byref(si), int(iterations), darr, nd,
+                               _stream(stream)))
     return dst
+
+
+def _morph(kind, src, dst, radius, stream, defines):
+    """Radius r = r successive launches of the r=1 kernel."""
+    dst = _out(src, dst)
+    return morphology(kind + _suffix(src), src, dst, int(radius), defines, stream)
 
 
 def erode_box(src, dst=None, radius=1, stream=None, defines=None):

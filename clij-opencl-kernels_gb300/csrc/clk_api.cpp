@@ -382,6 +382,7 @@ clk_status clk_separable(const char* kernel_name, const clk_image* dst_img, cons
   if ((st = device_ready())) return st;
   st = fused_separable(op, dst, src, taps, skip, pol, stm);
   if (st != CLK_UNSUPPORTED_DTYPE) return st;
+  st = CLK_OK;
 
   // Multi-pass: X, Y(, Z) with dst-typed temporaries, as three launches of
   // the reference kernels would run.
@@ -407,6 +408,56 @@ clk_status clk_separable(const char* kernel_name, const clk_image* dst_img, cons
   }
   for (int i = 0; i < 2; ++i)
     if (tmp[i]) cudaFreeAsync(tmp[i], stm);
+  return st;
+}
+
+clk_status clk_morphology(const char* kernel_name, const clk_image* dst_img, const clk_image* src_img,
+                          int32_t iterations, const clk_define* defines, size_t ndefines, void* stream) {
+  t_error.clear();
+  const KernelInfo* k = find_kernel(kernel_name);
+  if (!k) return fail(CLK_UNKNOWN_KERNEL, "unknown kernel '%s'", kernel_name ? kernel_name : "(null)");
+  if (k->fam != F_MORPH) return fail(CLK_BAD_ARG, "%s is not a morphology kernel", k->name);
+  if (!dst_img || !src_img) return fail(CLK_BAD_ARG, "null argument");
+  if (iterations < 0) return fail(CLK_BAD_ARG, "%s: iterations must be >= 0, got %d", k->name, iterations);
+  Policy pol;
+  clk_status st = parse_defines(defines, ndefines, &pol);
+  if (st) return st;
+  Image src, dst;
+  if ((st = to_image(*src_img, k->ndim, "src", &src))) return st;
+  if ((st = to_image(*dst_img, k->ndim, "dst", &dst))) return st;
+  if (src.w != dst.w || src.h != dst.h || src.d != dst.d)
+    return fail(CLK_BAD_ARG, "%s: src and dst extents differ", k->name);
+  if ((st = device_ready())) return st;
+  cudaStream_t stm = (cudaStream_t)stream;
+  const bool erode = (k->sub & 2) != 0, sphere = (k->sub & 1) != 0;
+  const Range r{dst.w, dst.h, dst.d};
+  if (iterations == 0) return direct_copy(dst, src, r, pol, stm);
+  // Each launch reads the previous result (dst-typed, like the orchestrator's
+  // temporaries).  Pairs of iterations run fused where the pixel types and
+  // layout allow; the chain of steps ping-pongs between a temporary and dst
+  // so that the last step writes dst and no step reads what it writes.
+  const bool fuse = fast_morph_fusable(dst, src);
+  const int nsteps = fuse ? (iterations + 1) / 2 : iterations;
+  void* tmp = nullptr;
+  if (nsteps > 1) {
+    const size_t bytes = (size_t)dst.count() * dtype_size(dst.dt);
+    if (cudaMallocAsync(&tmp, bytes, stm) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(CLK_OOM, "%s: cannot allocate a %zu-byte temporary", k->name, bytes);
+    }
+  }
+  Image cur = src;
+  int left = iterations;
+  for (int i = 0; i < nsteps && st == CLK_OK; ++i) {
+    Image out = dst;
+    if (i != nsteps - 1) out.ptr = ((nsteps - 1 - i) % 2 == 1) ? tmp : dst.ptr;
+    const int take = (fuse && left >= 2) ? 2 : 1;
+    st = fast_morph(erode, sphere, take, out, cur, pol, stm);
+    if (st == CLK_UNSUPPORTED_DTYPE && take == 1) st = direct_morph(erode, sphere, out, cur, r, pol, stm);
+    left -= take;
+    cur = out;
+  }
+  if (tmp) cudaFreeAsync(tmp, stm);
   return st;
 }
 

@@ -86,6 +86,7 @@ clk_status fused_separable(SepOp op, const Image& dst, const Image& src, const S
                            const Policy& p, cudaStream_t st);
 clk_status fast_morph(bool erode, bool sphere, int iterations, const Image& dst, const Image& src, const Policy& p,
                       cudaStream_t st);
+bool fast_morph_fusable(const Image& dst, const Image& src);  // fast_morph takes iterations = 2
 clk_status fast_sobel(const Image& dst, const Image& src, const Policy& p, cudaStream_t st);
 clk_status fast_median(bool sphere, const Image& dst, const Image& src, const MedianNbhd& m, cudaStream_t st);
 

@@ -142,6 +142,20 @@ clk_status clk_separable(const char* kernel_name, const clk_image* dst,
                          const float s[3], const clk_define* defines,
                          size_t ndefines, void* stream);
 
+/* ---------------------------------------------------------------------
+ * Orchestrator convenience: `iterations` successive launches of one of the
+ * r=1 morphology kernels erode/dilate_{box,sphere}_{2d,3d} (which have no
+ * radius parameter, erode_sphere_3d_x.cl:3-6) -- the radius-r request of
+ * the orchestrator.  The result equals that many clk_execute launches, each
+ * reading the previous result with clamp-to-edge; for byte images two
+ * iterations run fused in one pass.  iterations = 0 is a converting copy.
+ * Replaces: the host loop over the r=1 kernel (not in the reference).
+ * ------------------------------------------------------------------- */
+clk_status clk_morphology(const char* kernel_name, const clk_image* dst,
+                          const clk_image* src, int32_t iterations,
+                          const clk_define* defines, size_t ndefines,
+                          void* stream);
+
 /* Is kernel_name available for this (src, dst) pixel-type pair and ndim?
  * Returns 1 if yes, 0 if no. */
 int clk_supported(const char* kernel_name, int32_t src_dtype,
