@@ -256,6 +256,37 @@ int slot_of(const KernelInfo& k, const char* nm) {
 }
 
 }  // namespace
+
+clk_status separable_plan(const char* kernel_name, const clk_image* dst_img, const clk_image* src_img,
+                          const int32_t N[3], const float s[3], const clk_define* defines, size_t ndefines,
+                          SepPlan* plan) {
+  const KernelInfo* k = find_kernel(kernel_name);
+  if (!k) return fail(CLK_UNKNOWN_KERNEL, "unknown kernel '%s'", kernel_name ? kernel_name : "(null)");
+  if (k->fam != F_SEP) return fail(CLK_BAD_ARG, "%s is not a separable kernel", k->name);
+  if (!dst_img || !src_img || !N || !s) return fail(CLK_BAD_ARG, "null argument");
+  plan->pol = Policy{};
+  clk_status st = parse_defines(defines, ndefines, &plan->pol);
+  if (st) return st;
+  if ((st = to_image(*src_img, k->ndim, "src", &plan->src))) return st;
+  if ((st = to_image(*dst_img, k->ndim, "dst", &plan->dst))) return st;
+  if (plan->src.w != plan->dst.w || plan->src.h != plan->dst.h || plan->src.d != plan->dst.d)
+    return fail(CLK_BAD_ARG, "%s: src and dst extents differ", k->name);
+  plan->op = (SepOp)k->sub;
+  plan->ndim = k->ndim;
+  for (int d = 0; d < 3; ++d) {
+    plan->skip[d] = d >= k->ndim || N[d] <= 1 || (plan->op == SEP_GAUSS && !(s[d] > 0));
+    if (plan->skip[d]) {
+      box_taps(1, &plan->taps[d]);
+    } else if (plan->op == SEP_GAUSS) {
+      if (!gauss_taps(N[d], s[d], &plan->taps[d]))
+        return fail(CLK_BAD_ARG, "%s: N[%d]=%d exceeds %d taps", k->name, d, N[d], kMaxTaps);
+    } else {
+      box_taps(N[d], &plan->taps[d]);
+    }
+  }
+  return device_ready();
+}
+
 }  // namespace clk
 
 using namespace clk;
@@ -315,7 +346,9 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
       if ((st = device_ready())) return st;
       const bool full = r.x == dst.w && r.y == dst.h && r.z == dst.d && src.w == dst.w && src.h == dst.h &&
                         src.d == dst.d;
-      if (full) {
+      // float windows holding both -0 and +0 (or NaN) may pick the other zero
+      // on the network path; CLK_EXACT_ORDER keeps the insertion sort for them
+      if (full && !(pol.exact_order && src.dt == CLK_F32)) {
         st = fast_median(k->sub != 0, dst, src, m, s);
         if (st != CLK_UNSUPPORTED_DTYPE) return st;
       }

@@ -70,6 +70,19 @@ bool gauss_taps(int N, float s, SepTaps* t);  // false: window too large
 void box_taps(int N, SepTaps* t);
 bool median_nbhd(bool sphere, int ndim, int Nx, int Ny, int Nz, MedianNbhd* m);
 
+// The validated inputs of a whole separable filter (the checks of
+// clk_separable): kernel, images, policy, per-axis taps and skipped axes.
+struct SepPlan {
+  SepOp op;
+  int ndim;
+  Image dst, src;
+  Policy pol;
+  bool skip[3];
+  SepTaps taps[3];
+};
+clk_status separable_plan(const char* kernel_name, const clk_image* dst, const clk_image* src, const int32_t N[3],
+                          const float s[3], const clk_define* defines, size_t ndefines, SepPlan* plan);
+
 // ---- generic ("direct") kernels: one thread per output voxel, every
 // pixel-type pair, the reference's own evaluation order (bit-exact).
 clk_status direct_sep_pass(SepOp op, const Image& dst, const Image& src, int dim, const SepTaps& taps, Range r,

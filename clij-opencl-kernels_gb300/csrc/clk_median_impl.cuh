@@ -1,0 +1,269 @@
+// clk_median_impl.cuh - device code of the network medians (see clk_median.cu):
+// lane types, pixel-pair access, the tile bodies and their kernels.  Shared
+// by the plain launcher and the batch engine.
+#pragma once
+#include "clk_common.cuh"
+#include "clk_median_networks.cuh"
+
+namespace clk {
+namespace med {
+
+// Two 16-bit lanes with unsigned or signed order.
+template <bool SIGNED> struct Lanes {
+  uint32_t v;
+};
+template <bool S> __device__ __forceinline__ Lanes<S> vmin(Lanes<S> a, Lanes<S> b) {
+  Lanes<S> d;
+  if constexpr (S) asm("min.s16x2 %0, %1, %2;" : "=r"(d.v) : "r"(a.v), "r"(b.v));
+  else asm("min.u16x2 %0, %1, %2;" : "=r"(d.v) : "r"(a.v), "r"(b.v));
+  return d;
+}
+template <bool S> __device__ __forceinline__ Lanes<S> vmax(Lanes<S> a, Lanes<S> b) {
+  Lanes<S> d;
+  if constexpr (S) asm("max.s16x2 %0, %1, %2;" : "=r"(d.v) : "r"(a.v), "r"(b.v));
+  else asm("max.u16x2 %0, %1, %2;" : "=r"(d.v) : "r"(a.v), "r"(b.v));
+  return d;
+}
+
+// Two order-preserving 32-bit keys of float pixels: the bits with the sign
+// flipped for non-negative values and all bits flipped for negative ones, so
+// unsigned order is float order (with -0 below +0 and NaNs at the ends).
+struct Keys {
+  uint32_t lo, hi;
+};
+__device__ __forceinline__ Keys vmin(Keys a, Keys b) { return Keys{min(a.lo, b.lo), min(a.hi, b.hi)}; }
+__device__ __forceinline__ Keys vmax(Keys a, Keys b) { return Keys{max(a.lo, b.lo), max(a.hi, b.hi)}; }
+__device__ __forceinline__ uint32_t fkey(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fval(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+// Pixel pairs (x, x+1) as network values: load/store, and the lane shuffles
+// row_cols needs: lolo = (b.lo, b.lo), hihi = (b.hi, b.hi), hilo = (l.hi, b.lo).
+template <class T> struct Px;
+template <bool SG, int BYTES> struct Px16 {
+  typedef Lanes<SG> V;
+  static __device__ __forceinline__ V load(const void* row, int x) {
+    V v;
+    if constexpr (BYTES == 2) {
+      v.v = __ldg(reinterpret_cast<const uint32_t*>(row) + x / 2);
+    } else {
+      const uint32_t w = __ldg(reinterpret_cast<const uint16_t*>(row) + x / 2);
+      v.v = SG ? __byte_perm(w, 0, 0x9180) : __byte_perm(w, 0, 0x4140);
+    }
+    return v;
+  }
+  static __device__ __forceinline__ void store(void* row, int x, V v) {
+    if constexpr (BYTES == 2) reinterpret_cast<uint32_t*>(row)[x / 2] = v.v;
+    else reinterpret_cast<uint16_t*>(row)[x / 2] = (uint16_t)__byte_perm(v.v, 0, 0x0020);
+  }
+  static __device__ __forceinline__ V lolo(V b) { return V{__byte_perm(b.v, 0, 0x1010)}; }
+  static __device__ __forceinline__ V hihi(V b) { return V{__byte_perm(b.v, 0, 0x3232)}; }
+  static __device__ __forceinline__ V hilo(V l, V b) { return V{__byte_perm(l.v, b.v, 0x5432)}; }
+};
+template <> struct Px<uint16_t> : Px16<false, 2> {};
+template <> struct Px<int16_t> : Px16<true, 2> {};
+template <> struct Px<uint8_t> : Px16<false, 1> {};
+template <> struct Px<int8_t> : Px16<true, 1> {};
+template <> struct Px<float> {
+  typedef Keys V;
+  static __device__ __forceinline__ V load(const void* row, int x) {
+    const float2 f = __ldg(reinterpret_cast<const float2*>(row) + x / 2);
+    return Keys{fkey(f.x), fkey(f.y)};
+  }
+  static __device__ __forceinline__ void store(void* row, int x, V v) {
+    reinterpret_cast<float2*>(row)[x / 2] = make_float2(fval(v.lo), fval(v.hi));
+  }
+  static __device__ __forceinline__ V lolo(V b) { return Keys{b.lo, b.lo}; }
+  static __device__ __forceinline__ V hihi(V b) { return Keys{b.hi, b.hi}; }
+  static __device__ __forceinline__ V hilo(V l, V b) { return Keys{l.hi, b.lo}; }
+};
+
+template <class T> __device__ __forceinline__ typename Px<T>::V load_pair(const T* row, int x) {
+  return Px<T>::load(row, x);
+}
+template <class T> __device__ __forceinline__ void store_pair(T* row, int x, typename Px<T>::V v) {
+  Px<T>::store(row, x, v);
+}
+
+// Values for the columns x-1, x, x+1 of the pair's outputs in one row:
+// a = (x-1, x), b = (x, x+1), c = (x+1, x+2), clamped at the row ends; far_l
+// = (x-2, x-1) and far_r = (x+2, x+3), also clamped.
+template <class T, class V = typename Px<T>::V>
+__device__ __forceinline__ void row_cols(const T* row, int x, int W, V& a, V& b, V& c, V* far_l = nullptr,
+                                         V* far_r = nullptr) {
+  b = load_pair(row, x);
+  const V l = x >= 2 ? load_pair(row, x - 2) : Px<T>::lolo(b);
+  const V r = x + 2 < W ? load_pair(row, x + 2) : Px<T>::hihi(b);
+  a = Px<T>::hilo(l, b);
+  c = Px<T>::hilo(b, r);
+  if (far_l) *far_l = l;
+  if (far_r) *far_r = r;
+}
+
+template <class V, int N, int M> __device__ __forceinline__ void pick(const V (&w)[N], const int (&idx)[M], V (&o)[M]) {
+#pragma unroll
+  for (int k = 0; k < M; ++k) o[k] = w[idx[k]];
+}
+
+// Sorted 9 of the 3x3 block of plane (rows y-1..y+1, columns x-1..x+1) for
+// both lanes, plus optionally the extra values the sphere needs.
+template <class T, class V>
+__device__ __forceinline__ void block9(const T* plane, int x, int y, int W, int H, V (&p)[9]) {
+  V w[9];
+#pragma unroll
+  for (int dy = -1; dy <= 1; ++dy) {
+    const T* row = plane + (int64_t)clampi(y + dy, H - 1) * W;
+    row_cols<T>(row, x, W, w[dy + 1], w[dy + 4], w[dy + 7]);
+  }
+  {
+    V t[3] = {w[0], w[1], w[2]};
+    net_sort3_raw(t);
+    w[0] = t[net_sort3_out[0]], w[1] = t[net_sort3_out[1]], w[2] = t[net_sort3_out[2]];
+  }
+  {
+    V t[3] = {w[3], w[4], w[5]};
+    net_sort3_raw(t);
+    w[3] = t[net_sort3_out[0]], w[4] = t[net_sort3_out[1]], w[5] = t[net_sort3_out[2]];
+  }
+  {
+    V t[3] = {w[6], w[7], w[8]};
+    net_sort3_raw(t);
+    w[6] = t[net_sort3_out[0]], w[7] = t[net_sort3_out[1]], w[8] = t[net_sort3_out[2]];
+  }
+  net_merge333_raw(w);
+  pick(w, net_merge333_out, p);
+}
+
+template <class V> __device__ __forceinline__ void merge_mid(const V (&a)[9], const V (&b)[9], V (&m)[10]) {
+  V w[18];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) w[k] = a[k], w[9 + k] = b[k];
+  net_merge99_mid_raw(w);
+  pick(w, net_merge99_mid_out, m);
+}
+
+template <class V> __device__ __forceinline__ V final27(const V (&m)[10], const V (&p)[9]) {
+  V w[19];
+#pragma unroll
+  for (int k = 0; k < 10; ++k) w[k] = m[k];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) w[10 + k] = p[k];
+  net_box27_final_raw(w);
+  return w[net_box27_final_out[0]];
+}
+
+constexpr int BX = 32;  // threads (= pairs) per row of a tile
+constexpr int BY = 8;   // rows per tile
+
+// Tile bodies: tile (bx, by) x z-chunk bz, threads of a 256-thread CTA map to
+// BX pairs x BY rows.
+template <class T>
+__device__ __forceinline__ void box27_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int D,
+                                           int zchunk, int bx, int by, int bz) {
+  using V = typename Px<T>::V;
+  const int x = 2 * (bx * BX + (int)threadIdx.x % BX);
+  const int y = by * BY + (int)threadIdx.x / BX;
+  if (x >= W || y >= H) return;
+  const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+  V pm1[9], p0[9];
+  block9<T>(src + (int64_t)clampi(z0 - 1, D - 1) * plane, x, y, W, H, pm1);
+  block9<T>(src + (int64_t)z0 * plane, x, y, W, H, p0);
+  for (int zo = z0; zo < z1; zo += 2) {
+    V p1[9], p2[9], m[10];
+    block9<T>(src + (int64_t)clampi(zo + 1, D - 1) * plane, x, y, W, H, p1);
+    block9<T>(src + (int64_t)clampi(zo + 2, D - 1) * plane, x, y, W, H, p2);
+    merge_mid(p0, p1, m);
+    store_pair(dst + (int64_t)zo * plane + (int64_t)y * W, x, final27(m, pm1));
+    if (zo + 1 < z1) store_pair(dst + (int64_t)(zo + 1) * plane + (int64_t)y * W, x, final27(m, p2));
+#pragma unroll
+    for (int k = 0; k < 9; ++k) pm1[k] = p1[k], p0[k] = p2[k];
+  }
+}
+
+// median_sphere_3d with Nx = Ny = Nz = 5: per output the 3x3 blocks of
+// planes z-1, z, z+1, the four voxels at distance 2 in plane z and the two
+// at distance 2 along z (33 = 9 + 9 + 9 + 4 + 2).
+template <class T>
+__device__ __forceinline__ void sphere33_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int D,
+                                              int zchunk, int bx, int by, int bz) {
+  using V = typename Px<T>::V;
+  const int x = 2 * (bx * BX + (int)threadIdx.x % BX);
+  const int y = by * BY + (int)threadIdx.x / BX;
+  if (x >= W || y >= H) return;
+  const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+  auto centre = [&](int z) { return load_pair(src + (int64_t)clampi(z, D - 1) * plane + (int64_t)y * W, x); };
+  V pm1[9], p0[9];
+  block9<T>(src + (int64_t)clampi(z0 - 1, D - 1) * plane, x, y, W, H, pm1);
+  block9<T>(src + (int64_t)z0 * plane, x, y, W, H, p0);
+  V cm2 = centre(z0 - 2);
+  for (int zo = z0; zo < z1; ++zo) {
+    V p1[9];
+    const T* pz = src + (int64_t)clampi(zo + 1, D - 1) * plane;
+    block9<T>(pz, x, y, W, H, p1);
+    const T* pc = src + (int64_t)zo * plane;
+    V w[33];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) w[k] = pm1[k], w[9 + k] = p1[k], w[18 + k] = p0[k];
+    {
+      V a, b, c;
+      row_cols<T>(pc + (int64_t)y * W, x, W, a, b, c, &w[27], &w[28]);
+      w[29] = load_pair(pc + (int64_t)clampi(y - 2, H - 1) * W, x);
+      w[30] = load_pair(pc + (int64_t)clampi(y + 2, H - 1) * W, x);
+    }
+    w[31] = cm2;
+    w[32] = centre(zo + 2);
+    const V cm1 = centre(zo - 1);
+    net_sphere33_final_raw(w);
+    store_pair(dst + (int64_t)zo * plane + (int64_t)y * W, x, w[net_sphere33_final_out[0]]);
+    cm2 = cm1;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) pm1[k] = p0[k], p0[k] = p1[k];
+  }
+}
+
+// median_box_2d 3x3.
+template <class T>
+__device__ __forceinline__ void box9_2d_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int bx,
+                                             int by) {
+  using V = typename Px<T>::V;
+  const int x = 2 * (bx * BX + (int)threadIdx.x % BX);
+  const int y = by * BY + (int)threadIdx.x / BX;
+  if (x >= W || y >= H) return;
+  V w[9];
+#pragma unroll
+  for (int dy = -1; dy <= 1; ++dy) row_cols<T>(src + (int64_t)clampi(y + dy, H - 1) * W, x, W, w[dy + 1], w[dy + 4], w[dy + 7]);
+#pragma unroll
+  for (int col = 0; col < 3; ++col) {
+    V t[3] = {w[3 * col], w[3 * col + 1], w[3 * col + 2]};
+    net_sort3_raw(t);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) w[3 * col + k] = t[net_sort3_out[k]];
+  }
+  net_med9_raw(w);
+  store_pair(dst + (int64_t)y * W, x, w[net_med9_out[0]]);
+}
+
+template <class T>
+__global__ void __launch_bounds__(BX * BY) k_median_box27(const T* __restrict__ src, T* __restrict__ dst, int W,
+                                                          int H, int D, int zchunk) {
+  box27_tile<T>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+template <class T>
+__global__ void __launch_bounds__(BX * BY) k_median_sphere33(const T* __restrict__ src, T* __restrict__ dst, int W,
+                                                             int H, int D, int zchunk) {
+  sphere33_tile<T>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+template <class T>
+__global__ void __launch_bounds__(BX * BY) k_median_box9_2d(const T* __restrict__ src, T* __restrict__ dst, int W,
+                                                            int H) {
+  box9_2d_tile<T>(src, dst, W, H, blockIdx.x, blockIdx.y);
+}
+
+}  // namespace med
+}  // namespace clk

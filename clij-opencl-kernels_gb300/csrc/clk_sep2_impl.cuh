@@ -48,19 +48,21 @@ template <class S, int OP, int R> struct Geo {
   static size_t smem(int cz) { return tin_bytes() + xs_bytes() + ring_bytes(cz); }
 };
 
+// One tile (bx, by) x z-chunk bz of one image; the whole CTA takes part.
+// smem: dynamic shared memory of at least Geo::smem(p.cz) bytes.
 template <class S, class D, int OP, int R>
-__global__ void __launch_bounds__(NT) k_sep2(const S* __restrict__ src, D* __restrict__ dst, int W, int H, int Dz,
-                                             int zchunk, const __grid_constant__ Params p) {
+__device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restrict__ dst, int W, int H, int Dz,
+                                          int zchunk, const Params& p, int bx, int by, int bz,
+                                          unsigned char* smem) {
   using G = Geo<S, OP, R>;
   using T = typename G::T;
-  extern __shared__ __align__(16) unsigned char smem[];
   S* tin = reinterpret_cast<S*>(smem);
   T* xs = reinterpret_cast<T*>(smem + G::tin_bytes());
   T* ring = reinterpret_cast<T*>(smem + G::tin_bytes() + G::xs_bytes());
   const int cz = p.cz, NZ = 2 * cz + 1;
   const int tid = threadIdx.x;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int z0 = blockIdx.z * zchunk, z1 = min(Dz, z0 + zchunk);
+  const int x0 = bx * TX, y0 = by * TY;
+  const int z0 = bz * zchunk, z1 = min(Dz, z0 + zchunk);
   const int64_t plane = (int64_t)W * H;
 
   S pre[G::PER];
@@ -259,6 +261,13 @@ __global__ void __launch_bounds__(NT) k_sep2(const S* __restrict__ src, D* __res
       }
     }
   }
+}
+
+template <class S, class D, int OP, int R>
+__global__ void __launch_bounds__(NT) k_sep2(const S* __restrict__ src, D* __restrict__ dst, int W, int H, int Dz,
+                                             int zchunk, const __grid_constant__ Params p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  sep2_tile<S, D, OP, R>(src, dst, W, H, Dz, zchunk, p, blockIdx.x, blockIdx.y, blockIdx.z, smem);
 }
 
 template <class S, class D, int OP, int R>

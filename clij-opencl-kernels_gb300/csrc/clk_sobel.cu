@@ -1,5 +1,195 @@
-// clk_sobel.cu - tiled Sobel (placeholder).
+// clk_sobel.cu - fast sobel_3d (sobel_3d_x.cl:3-57) to float.
+//
+// The kernel's 3x3x4 window (dz = -1..+2, the k<=3 loop reading the flat
+// arrays one row on, the last tap pinned to 0) decomposes per input plane
+// into row sums sx = v(x-1) + 2v(x) + v(x+1) and differences
+// dx = v(x-1) - v(x+1):
+//   A = dx(y-1) + 2dx(y) + dx(y+1)   B = sx(y-1) - sx(y+1)
+//   C = sx(y-1) + 2sx(y) + sx(y+1)   q = 2v(x-1,y+1) + v(x,y+1)
+//   Ex = 2dx(y-1) + dx(y) - v(x,y+1) Ey = q - sx(y)   Ez = 2sx(y-1) + sx(y) + q
+// and then along z
+//   Sx = A(z-1) + 2A(z) + A(z+1) + Ex(z+2)
+//   Sy = B(z-1) + 2B(z) + B(z+1) + Ey(z+2)
+//   Sz = C(z-1) - C(z+1) + Ez(z+2),
+// exact integer sums for integer pixels.  For unsigned pixels the kernel
+// multiplies int coefficients by uint reads (C: the product is uint), so
+// each negative-coefficient tap with a nonzero pixel contributes 2^32 more:
+// sum_c = S_c + K_c * 2^32 with K_c the count of such taps (12, 12, 9 when no
+// pixel of the window is 0; counted exactly otherwise).  The float result
+// sqrt(sx^2 + sy^2 + sz^2) is within 1e-5 of the FP64 evaluation; integer
+// outputs use the generic kernel, which sums in the reference's order.
+//
+// A thread owns 2 x 2 outputs (x, x+1; y, y+1) and walks along z, keeping
+// A, B, C of the last three planes in registers.
 #include "clk_common.cuh"
+
 namespace clk {
-clk_status fast_sobel(const Image&, const Image&, const Policy&, cudaStream_t) { return CLK_UNSUPPORTED_DTYPE; }
+
+namespace {
+
+constexpr int SBX = 32, SBY = 8;  // threads: 64 columns x 16 rows per block
+
+template <class S> struct Num { typedef int type; };
+template <> struct Num<float> { typedef float type; };
+
+// v(x-1), v(x), v(x+1), v(x+2) of one row, clamped at the row ends
+template <class S>
+__device__ __forceinline__ void load4(const S* row, int x, int W, typename Num<S>::type (&v)[4]) {
+  using N = typename Num<S>::type;
+  v[0] = (N)__ldg(row + (x > 0 ? x - 1 : 0));
+  v[1] = (N)__ldg(row + x);
+  v[2] = (N)__ldg(row + min(x + 1, W - 1));
+  v[3] = (N)__ldg(row + min(x + 2, W - 1));
+}
+
+// Exact counts K of the negative-coefficient taps with a nonzero pixel
+// (unsigned reads), for a window that contains a zero pixel.
+template <class S>
+__device__ __noinline__ float3 wrap_counts(const S* __restrict__ src, int W, int H, int D, int gx, int gy, int z) {
+  const Dims3 dm{W, H, D};
+  auto nz = [&](int ddx, int ddy, int ddz) -> float {
+    return __ldg(src + atc(dm, gx + ddx, gy + ddy, z + ddz)) != 0 ? 1.f : 0.f;
+  };
+  float kx = 0.f, ky = 0.f, kz = 0.f;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int d = -1; d <= 1; ++d) {
+      kx += nz(1, d, dz);  // gx: dx = +1 taps
+      ky += nz(d, 1, dz);  // gy: dy = +1 taps
+    }
+  for (int ddx = -1; ddx <= 1; ++ddx)
+    for (int ddy = -1; ddy <= 1; ++ddy) kz += nz(ddx, ddy, 1);  // gz: dz = +1 taps
+  kx += nz(0, 1, 2) + nz(1, -1, 2) + nz(1, 0, 2);   // negative taps of the dz = +2 plane
+  ky += nz(-1, 0, 2) + nz(0, 0, 2) + nz(1, 0, 2);
+  return make_float3(kx, ky, kz);
+}
+
+template <class S, bool WRAP>
+__global__ void __launch_bounds__(SBX * SBY) k_sobel3d_fast(const S* __restrict__ src, float* __restrict__ dst, int W,
+                                                            int H, int D, int zchunk) {
+  using N = typename Num<S>::type;
+  const int x = 2 * (blockIdx.x * SBX + threadIdx.x);
+  const int y = 2 * (blockIdx.y * SBY + threadIdx.y);
+  if (x >= W || y >= H) return;
+  const int z0 = blockIdx.z * zchunk, z1 = min(D, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+
+  // per output (ox, oy): A, B, C of planes p-3, p-2, p-1 (ring index 0..2)
+  N A[3][2][2], B[3][2][2], C[3][2][2];
+  uint32_t zflags = 0;  // bit i: a zero pixel among this thread's loads of plane p-i
+
+  // partial sums of plane p; also returns the E terms
+  auto plane_terms = [&](int p, N (&a)[2][2], N (&b)[2][2], N (&c)[2][2], N (&ex)[2][2], N (&ey)[2][2],
+                         N (&ez)[2][2]) {
+    const S* sp = src + (int64_t)clampi(p, D - 1) * plane;
+    N v[4][4];  // rows y-1 .. y+2, columns x-1 .. x+2
+#pragma unroll
+    for (int r = 0; r < 4; ++r) load4<S>(sp + (int64_t)clampi(y - 1 + r, H - 1) * W, x, W, v[r]);
+    if constexpr (WRAP) {
+      bool z = false;
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) z |= v[r][c] == 0;
+      zflags = (zflags << 1) | (z ? 1u : 0u);
+    }
+    N sx[4][2], dx[4][2];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int o = 0; o < 2; ++o) {
+        sx[r][o] = v[r][o] + 2 * v[r][o + 1] + v[r][o + 2];
+        dx[r][o] = v[r][o] - v[r][o + 2];
+      }
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) {
+        const int rm = oy, rc = oy + 1, rp = oy + 2;
+        a[oy][ox] = dx[rm][ox] + 2 * dx[rc][ox] + dx[rp][ox];
+        b[oy][ox] = sx[rm][ox] - sx[rp][ox];
+        c[oy][ox] = sx[rm][ox] + 2 * sx[rc][ox] + sx[rp][ox];
+        const N q = 2 * v[rp][ox] + v[rp][ox + 1];
+        ex[oy][ox] = 2 * dx[rm][ox] + dx[rc][ox] - v[rp][ox + 1];
+        ey[oy][ox] = q - sx[rc][ox];
+        ez[oy][ox] = 2 * sx[rm][ox] + sx[rc][ox] + q;
+      }
+  };
+
+  N ex[2][2], ey[2][2], ez[2][2];
+  plane_terms(z0 - 1, A[0], B[0], C[0], ex, ey, ez);
+  plane_terms(z0, A[1], B[1], C[1], ex, ey, ez);
+  plane_terms(z0 + 1, A[2], B[2], C[2], ex, ey, ez);
+  for (int zo = z0; zo < z1; ++zo) {
+    N a[2][2], b[2][2], c[2][2];
+    plane_terms(zo + 2, a, b, c, ex, ey, ez);
+    float res[2][2];
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) {
+        const N sxv = A[0][oy][ox] + 2 * A[1][oy][ox] + A[2][oy][ox] + ex[oy][ox];
+        const N syv = B[0][oy][ox] + 2 * B[1][oy][ox] + B[2][oy][ox] + ey[oy][ox];
+        const N szv = C[0][oy][ox] - C[2][oy][ox] + ez[oy][ox];
+        float fx = (float)sxv, fy = (float)syv, fz = (float)szv;
+        if constexpr (WRAP) {
+          float kx = 12.f, ky = 12.f, kz = 9.f;
+          if (zflags & 0xFu) {  // a zero pixel in planes zo-1 .. zo+2: count exactly
+            const float3 k = wrap_counts<S>(src, W, H, D, x + ox, y + oy, zo);
+            kx = k.x, ky = k.y, kz = k.z;
+          }
+          fx = fmaf(kx, 4294967296.0f, fx);
+          fy = fmaf(ky, 4294967296.0f, fy);
+          fz = fmaf(kz, 4294967296.0f, fz);
+        }
+        res[oy][ox] = sqrtf(fmaf(fx, fx, fmaf(fy, fy, fz * fz)));
+      }
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy) {
+      if (y + oy < H)
+        *reinterpret_cast<float2*>(dst + (int64_t)zo * plane + (int64_t)(y + oy) * W + x) =
+            make_float2(res[oy][0], res[oy][1]);
+    }
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) {
+        A[0][oy][ox] = A[1][oy][ox], A[1][oy][ox] = A[2][oy][ox], A[2][oy][ox] = a[oy][ox];
+        B[0][oy][ox] = B[1][oy][ox], B[1][oy][ox] = B[2][oy][ox], B[2][oy][ox] = b[oy][ox];
+        C[0][oy][ox] = C[1][oy][ox], C[1][oy][ox] = C[2][oy][ox], C[2][oy][ox] = c[oy][ox];
+      }
+  }
+}
+
+template <class S, bool WRAP> clk_status launch_sobel(const Image& dst, const Image& src, cudaStream_t st) {
+  const dim3 block(SBX, SBY);
+  const int tx = (src.w / 2 + SBX - 1) / SBX, ty = ((src.h + 1) / 2 + SBY - 1) / SBY;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int chunks = 1;
+  while ((int64_t)tx * ty * chunks < 8LL * sms && src.d / (chunks * 2) >= 16) chunks *= 2;
+  const int zchunk = (src.d + chunks - 1) / chunks;
+  k_sobel3d_fast<S, WRAP><<<dim3(tx, ty, (src.d + zchunk - 1) / zchunk), block, 0, st>>>(
+      (const S*)src.ptr, (float*)dst.ptr, src.w, src.h, src.d, zchunk);
+  count_launch();
+  return check_launch("sobel_3d (fast)");
+}
+
+}  // namespace
+
+clk_status fast_sobel(const Image& dst, const Image& src, const Policy& p, cudaStream_t st) {
+  if (src.ndim != 3 || dst.dt != CLK_F32 || src.w % 2 != 0 || src.w != dst.w || src.h != dst.h || src.d != dst.d)
+    return CLK_UNSUPPORTED_DTYPE;
+  if ((uintptr_t)dst.ptr % 8 != 0) return CLK_UNSUPPORTED_DTYPE;
+  const bool wrap = !p.sobel_narrow;
+  switch (src.dt) {
+    case CLK_U16: return wrap ? launch_sobel<uint16_t, true>(dst, src, st) : launch_sobel<uint16_t, false>(dst, src, st);
+    case CLK_U8: return wrap ? launch_sobel<uint8_t, true>(dst, src, st) : launch_sobel<uint8_t, false>(dst, src, st);
+    case CLK_I16: return launch_sobel<int16_t, false>(dst, src, st);
+    case CLK_I8: return launch_sobel<int8_t, false>(dst, src, st);
+    case CLK_F32: return launch_sobel<float, false>(dst, src, st);
+  }
+  return CLK_UNSUPPORTED_DTYPE;
+}
+
 }  // namespace clk

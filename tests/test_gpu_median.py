@@ -35,7 +35,7 @@ CASES = [("median_box_3d", {"Nx": 3, "Ny": 3, "Nz": 3}), ("median_sphere_3d", {"
 
 
 @pytest.mark.parametrize("kernel,params", CASES)
-@pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.int8])
+@pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.int8, np.float32])
 def test_network_median_3d(clk, oracle, kernel, params, dt):
     rng = np.random.default_rng(23)
     for shp in ((21, 37, 130), (1, 5, 64), (2, 1, 2), (7, 64, 2), (33, 16, 66)):

@@ -1,0 +1,82 @@
+"""GPU parity of the fused separable kernels over the radii and layouts they
+specialise on: isotropic XY radii 1..8 (integer min/max/mean, bit-exact)
+and 1..12 (Gaussian to float, within the FP64 tolerance), even and odd
+widths, thin stacks, 2-D images, skipped axes."""
+import numpy as np
+import pytest
+
+from conftest import random_image
+
+pytestmark = pytest.mark.gpu
+REL_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def clk():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    import clk as m
+    m.load()
+    return m
+
+
+def run(clk, kernel, a, ddt, N, s):
+    import torch
+    from clk.api import torch_dtype
+    from oracle.oracle import dtype_code
+    d = torch.empty(a.shape, dtype=torch_dtype(dtype_code(ddt)), device="cuda")
+    clk.separable(kernel, torch.from_numpy(a).cuda(), d, N, s)
+    torch.cuda.synchronize()
+    return d.cpu().numpy()
+
+
+def close(got, val, scale):
+    err = np.abs(got.astype(np.float64) - val)
+    return (err <= REL_TOL * np.maximum(np.abs(val), scale)).all()
+
+
+@pytest.mark.parametrize("kernel", ["minimum_separable_3d", "maximum_separable_3d", "mean_separable_3d"])
+@pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.int8])
+def test_integer_isotropic_radii(clk, oracle, kernel, dt):
+    rng = np.random.default_rng(31)
+    for shp in ((19, 70, 130), (3, 33, 64), (1, 40, 66), (40, 8, 10)):
+        a = random_image(rng, shp, dt)
+        for R in range(1, 9):
+            for rz in (0, 1, R):
+                N = (2 * R + 1, 2 * R + 1, 2 * rz + 1)
+                want = oracle.separable(kernel, a, dt, N, (R, R, rz))
+                got = run(clk, kernel, a, dt, N, (R, R, rz))
+                assert np.array_equal(got, want), (kernel, shp, np.dtype(dt), N)
+
+
+@pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.float32])
+def test_gaussian_to_float_isotropic(clk, oracle, dt):
+    rng = np.random.default_rng(32)
+    for shp in ((17, 70, 130), (2, 35, 64)):
+        a = random_image(rng, shp, dt)
+        for R in (1, 3, 6, 9, 12):
+            sig = R / 3.0
+            for sz in (0.0, 0.7, 1.5):
+                N = (2 * R + 1, 2 * R + 1, 2 * int(np.ceil(3 * sz)) + 1 if sz > 0 else 1)
+                s = (sig, sig, sz)
+                val, scale = oracle.fp64("gaussian_blur_separable_3d", a, N, s)
+                got = run(clk, "gaussian_blur_separable_3d", a, np.float32, N, s)
+                assert close(got, val, scale), (shp, np.dtype(dt), N, s)
+
+
+def test_2d_and_config_shapes(clk, oracle):
+    rng = np.random.default_rng(33)
+    a2 = random_image(rng, (96, 130), np.uint16)
+    for kernel in ("minimum_separable_2d", "maximum_separable_2d", "mean_separable_2d"):
+        want = oracle.separable(kernel, a2, np.uint16, (9, 9), (4, 4))
+        assert np.array_equal(run(clk, kernel, a2, np.uint16, (9, 9), (4, 4)), want)
+    val, scale = oracle.fp64("gaussian_blur_separable_2d", a2, (13, 13), (2.0, 2.0))
+    assert close(run(clk, "gaussian_blur_separable_2d", a2, np.float32, (13, 13), (2.0, 2.0)), val, scale)
+    # the headline configurations on a thin slab of the same shape family
+    a = random_image(rng, (12, 64, 256), np.uint16)
+    for kernel in ("mean_separable_3d", "minimum_separable_3d", "maximum_separable_3d"):
+        want = oracle.separable(kernel, a, np.uint16, (11, 11, 5), (5, 5, 2))
+        assert np.array_equal(run(clk, kernel, a, np.uint16, (11, 11, 5), (5, 5, 2)), want), kernel
+    val, scale = oracle.fp64("gaussian_blur_separable_3d", a, (19, 19, 11), (3.0, 3.0, 1.5))
+    assert close(run(clk, "gaussian_blur_separable_3d", a, np.float32, (19, 19, 11), (3.0, 3.0, 1.5)), val, scale)
