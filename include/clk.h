@@ -143,6 +143,26 @@ clk_status clk_separable(const char* kernel_name, const clk_image* dst,
                          size_t ndefines, void* stream);
 
 /* ---------------------------------------------------------------------
+ * clk_separable for callers that cannot let the library allocate device
+ * memory: a host application that owns the whole device-memory budget and
+ * forbids allocations it does not make itself, a loop that must not stall
+ * or fail with out-of-memory halfway through, or a plugin whose host
+ * manages all GPU memory.  This entry point has no counterpart in the
+ * reference.
+ * Same arguments, results and errors as clk_separable, computed pass by
+ * pass; the two temporaries come from one fixed array in device memory
+ * (64 MiB, held by every GPU that loads the library until the process
+ * exits), so a call allocates nothing.  Limit: dst voxels x dst pixel size
+ * must be at most 32 MiB, else CLK_BAD_ARG.  The first call on each device
+ * looks up the array's device address (make it outside any stream
+ * capture).  Calls share the array: calls that overlap on the GPU race.
+ * ------------------------------------------------------------------- */
+clk_status clk_separable_noalloc(const char* kernel_name, const clk_image* dst,
+                                 const clk_image* src, const int32_t N[3],
+                                 const float s[3], const clk_define* defines,
+                                 size_t ndefines, void* stream);
+
+/* ---------------------------------------------------------------------
  * Orchestrator convenience: `iterations` successive launches of one of the
  * r=1 morphology kernels erode/dilate_{box,sphere}_{2d,3d} (which have no
  * radius parameter, erode_sphere_3d_x.cl:3-6) -- the radius-r request of
