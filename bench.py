@@ -175,6 +175,184 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def batch_images(n=512, seed=3, device="cuda"):
+    """The uneven batch: 40% u8 / 40% u16 / 20% f32; half 2-D with X, Y
+    log-uniform in [64, 1024], half 3-D with X, Y log-uniform in [64, 512]
+    and Z uniform in [16, 128]; blob density of the 1024x1024x256 stack,
+    intensities scaled to the pixel type's range."""
+    import numpy as np
+    import torch
+
+    from clk import synth
+
+    rng = np.random.default_rng(seed)
+    density = N_BLOBS / float(SHAPE[0] * SHAPE[1] * SHAPE[2])
+    imgs = []
+    for k in range(n):
+        u = rng.random()
+        dt = torch.uint8 if u < 0.4 else (torch.uint16 if u < 0.8 else torch.float32)
+        if k % 2 == 0:
+            shp = tuple(int(np.exp(rng.uniform(np.log(64), np.log(1024)))) for _ in range(2))
+        else:
+            xy = [int(np.exp(rng.uniform(np.log(64), np.log(512)))) for _ in range(2)]
+            shp = (int(rng.integers(16, 129)), xy[0], xy[1])
+        nb = max(1, int(round(density * float(np.prod(shp)))))
+        imgs.append(synth.blobs(shp, nb, seed=seed * 100003 + k, dtype=dt, device=device, scale_to_dtype=True))
+    return imgs
+
+
+def run_batch(args):
+    """BASELINE config 3: the top-hat chain over the uneven batch, batched
+    (one graph launch) against per-image plain calls, same results."""
+    import torch
+
+    import clk
+
+    torch.cuda.set_device(0)
+    imgs = batch_images()
+    outs = [torch.empty_like(t) for t in imgs]
+    ops = [clk.op_separable("gaussian_blur_separable", (13, 13, 13), (2.0, 2.0, 2.0)),
+           clk.op_separable("minimum_separable", (9, 9, 9), (4.0, 4.0, 4.0)),
+           clk.op_separable("maximum_separable", (9, 9, 9), (4.0, 4.0, 4.0)),
+           clk.op_kernel("median_box", (3, 3, 3))]
+    t0 = time.perf_counter()
+    b = clk.Batch(ops, imgs, outs)
+    plan_s = time.perf_counter() - t0
+    vox = sum(t.numel() for t in imgs) * len(ops)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        lat = []
+        e0.record(stream)
+        for _ in range(args.steps):
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            z.record(stream)
+            lat.append((a, z))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps, [a.elapsed_time(z) for a, z in lat]
+
+    l0 = clk.launch_count()
+    ms_b, _ = timed(b.run)
+    launches_b = (clk.launch_count() - l0) // (args.steps + max(3, args.warmup))
+    batched = [t.clone() for t in outs]
+    l0 = clk.launch_count()
+    ms_p, _ = timed(b.run_plain)
+    launches_p = (clk.launch_count() - l0) // (args.steps + max(3, args.warmup))
+    same = all(torch.equal(x.view(torch.uint8) if x.dtype != torch.uint8 else x,
+                           y.view(torch.uint8) if y.dtype != torch.uint8 else y) for x, y in zip(batched, outs))
+    l0 = clk.launch_count()
+    ms_k, _ = timed(b.run_per_kernel)
+    launches_k = (clk.launch_count() - l0) // (args.steps + max(3, args.warmup))
+    n_u8 = sum(t.dtype == torch.uint8 for t in imgs)
+    n_u16 = sum(t.dtype == torch.uint16 for t in imgs)
+    line = {
+        "metric": "Gvoxel/s (batched pipeline, 512 uneven images)", "value": round(vox / (ms_b * 1e-3) / 1e9, 3),
+        "unit": "Gvoxel/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": round(ms_b, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u8/u16/f32 pixels, same type out", "data": "synthetic: seeded blob images, intensities scaled to type",
+        "config": {"workload": "config 3: 512 images (half 2-D XY in [64,1024], half 3-D XY in [64,512] x Z in "
+                               "[16,128]), top-hat chain gaussian s=2 -> minimum r=4 -> maximum r=4 -> median_box r=1",
+                   "images": len(imgs), "u8": n_u8, "u16": n_u16, "f32": len(imgs) - n_u8 - n_u16,
+                   "voxels_per_step": vox, "l2": "working set far larger than L2"},
+        "plain": {"value": round(vox / (ms_p * 1e-3) / 1e9, 3), "ms_per_step": round(ms_p, 4),
+                  "launches_per_step": launches_p, "what": "per image, whole-filter calls (clk_separable, "
+                                                           "clk_execute), one stream"},
+        "per_kernel": {"value": round(vox / (ms_k * 1e-3) / 1e9, 3), "ms_per_step": round(ms_k, 4),
+                       "launches_per_step": launches_k, "what": "per image, one clk_execute per kernel and axis "
+                                                                "(the reference's launch pattern)"},
+        "speedup_vs_plain": round(ms_p / ms_b, 3), "speedup_vs_per_kernel": round(ms_k / ms_b, 3), "gpu_launches": launches_b, "graph_kernels": b.launches,
+        "identical_to_plain": bool(same), "plan_and_autotune_s": round(plan_s, 2),
+    }
+    print(json.dumps(line))
+    b.close()
+
+
+def serve_pipeline(clk, rng):
+    """1-4 steps sampled uniformly from {gaussian s in [1,4], mean r in [1,5],
+    median_box r=1, erode/dilate_sphere r in [1,2], sobel}."""
+    import numpy as np
+    ops = []
+    for _ in range(int(rng.integers(1, 5))):
+        k = int(rng.integers(0, 5))
+        if k == 0:
+            s = float(rng.uniform(1, 4))
+            n = 2 * int(np.ceil(3 * s)) + 1
+            ops.append(clk.op_separable("gaussian_blur_separable", (n, n, n), (s, s, s)))
+        elif k == 1:
+            r = int(rng.integers(1, 6))
+            ops.append(clk.op_separable("mean_separable", (2 * r + 1,) * 3, (r, r, r)))
+        elif k == 2:
+            ops.append(clk.op_kernel("median_box", (3, 3, 3)))
+        elif k == 3:
+            ops.append(clk.op_morphology("erode_sphere" if rng.random() < 0.5 else "dilate_sphere",
+                                         int(rng.integers(1, 3))))
+        else:
+            ops.append(clk.op_kernel("sobel"))
+    return ops
+
+
+def run_serve(args):
+    """BASELINE config 4: Poisson arrivals at 200 / 1000 / 5000 req/s, each
+    request one stack from the config-3 size and type distribution and a
+    random 1-4 step pipeline, served with continuous admission (16 slots,
+    64 GiB budget) against the same arrivals served one at a time."""
+    import numpy as np
+    import torch
+
+    import clk
+
+    torch.cuda.set_device(0)
+    pool = batch_images(n=96, seed=5)
+    duration = 1.5
+    results = []
+    for rate in (200, 1000, 5000):
+        rng = np.random.default_rng(rate)
+        n = int(rate * duration)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+        reqs = [(serve_pipeline(clk, rng), pool[int(rng.integers(0, len(pool)))]) for _ in range(n)]
+        outs = [torch.empty_like(src) for _, src in reqs]
+        row = {"rate_req_s": rate, "requests": n}
+        for mode, slots in (("served", 16), ("serial", 1)):
+            srv = clk.Server(slots=slots, hbm_budget_bytes=64 << 30)
+            srv.wait(srv.submit(reqs[0][0], reqs[0][1], outs[0]))  # warm-up (not counted)
+            srv.close()
+            srv = clk.Server(slots=slots, hbm_budget_bytes=64 << 30)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            tickets = []
+            for k, ((ops, src), out) in enumerate(zip(reqs, outs)):
+                while time.perf_counter() - t0 < arrivals[k]:
+                    pass
+                tickets.append(srv.submit(ops, src, out))
+            srv.drain(600000)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+            srv.close()
+            row[mode] = {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                         "mean_ms": round(st["mean_ms"], 3), "gvox_s": round(st["voxel_steps"] / wall / 1e9, 3),
+                         "completed": int(st["completed"]), "failed": int(st["failed"]),
+                         "peak_temporaries_gib": round(st["bytes_peak"] / 2**30, 3), "wall_s": round(wall, 3)}
+        results.append(row)
+    top = results[-1]
+    line = {
+        "metric": "served p99 latency and Gvoxel/s (Poisson arrivals, config-3 stacks, 1-4 step pipelines)",
+        "value": top["served"]["p99_ms"], "unit": "ms (p99 at 5000 req/s)", "n_gpus": 1, "steps": len(results),
+        "warmup": 1, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u8/u16/f32 pixels, same type out", "data": "synthetic: 96 seeded blob stacks, random pipelines",
+        "config": {"workload": "config 4: continuous admission, 16 slots, 64 GiB budget for temporaries; serial "
+                               "= the same arrivals through 1 slot", "duration_s_per_rate": duration},
+        "rates": results,
+    }
+    print(json.dumps(line))
+
+
 def cpu_baseline(a_np, mask_np):
     """Reference CPU kernels on a bounded sample (first SAMPLE voxels)."""
     import numpy as np
@@ -213,9 +391,15 @@ def main():
     ap.add_argument("--full-sample", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="suite", choices=["suite", "batch", "serve"],
+                    help="suite: config 2 (default); batch: config 3; serve: config 4")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
 
     import torch
 

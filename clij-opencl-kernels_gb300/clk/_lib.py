@@ -35,6 +35,21 @@ class clk_define(C.Structure):
     _fields_ = [("name", C.c_char_p), ("value", C.c_char_p)]
 
 
+class clk_op(C.Structure):
+    _fields_ = [("kernel", C.c_char_p), ("kind", C.c_int32), ("N", C.c_int32 * 3), ("s", C.c_float * 3),
+                ("iterations", C.c_int32)]
+
+
+OP_SEPARABLE, OP_KERNEL, OP_MORPHOLOGY = range(3)
+
+
+class clk_server_stats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("bytes_in_use", C.c_int64), ("bytes_peak", C.c_int64), ("inflight", C.c_int32),
+                ("queued", C.c_int32), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
+                ("voxel_steps", C.c_double), ("busy_s", C.c_double)]
+
+
 class ClkError(RuntimeError):
     """A non-OK clk_status; .status holds the code."""
 
@@ -44,7 +59,10 @@ class ClkError(RuntimeError):
         self.status = status
 
 
-EXPORTS = ["clk_execute", "clk_separable", "clk_morphology", "clk_supported", "clk_last_error_string", "clk_version",
+EXPORTS = ["clk_execute", "clk_separable", "clk_separable_noalloc", "clk_morphology", "clk_batch_create",
+           "clk_batch_run", "clk_batch_run_plain", "clk_batch_run_per_kernel", "clk_batch_launches", "clk_batch_destroy", "clk_server_create",
+           "clk_server_submit", "clk_server_wait", "clk_server_drain", "clk_server_get_stats",
+           "clk_server_destroy", "clk_supported", "clk_last_error_string", "clk_version",
            "clk_kernel_count", "clk_kernel_name", "clk_launch_count"]
 
 _lib = None
@@ -67,6 +85,33 @@ def load() -> C.CDLL:
     lib.clk_morphology.argtypes = [C.c_char_p, C.POINTER(clk_image), C.POINTER(clk_image), C.c_int32,
                                    C.POINTER(clk_define), C.c_size_t, C.c_void_p]
     lib.clk_morphology.restype = C.c_int
+    lib.clk_batch_create.argtypes = [C.POINTER(clk_op), C.c_int32, C.POINTER(clk_image), C.POINTER(clk_image),
+                                     C.c_int32, C.POINTER(clk_define), C.c_size_t, C.c_void_p,
+                                     C.POINTER(C.c_void_p)]
+    lib.clk_batch_create.restype = C.c_int
+    lib.clk_batch_run.argtypes = [C.c_void_p, C.c_void_p]
+    lib.clk_batch_run.restype = C.c_int
+    lib.clk_batch_run_plain.argtypes = [C.c_void_p, C.c_void_p]
+    lib.clk_batch_run_plain.restype = C.c_int
+    lib.clk_batch_run_per_kernel.argtypes = [C.c_void_p, C.c_void_p]
+    lib.clk_batch_run_per_kernel.restype = C.c_int
+    lib.clk_batch_launches.argtypes = [C.c_void_p]
+    lib.clk_batch_launches.restype = C.c_int32
+    lib.clk_batch_destroy.argtypes = [C.c_void_p]
+    lib.clk_batch_destroy.restype = None
+    lib.clk_server_create.argtypes = [C.c_int32, C.c_int64, C.POINTER(C.c_void_p)]
+    lib.clk_server_create.restype = C.c_int
+    lib.clk_server_submit.argtypes = [C.c_void_p, C.POINTER(clk_op), C.c_int32, C.POINTER(clk_image),
+                                      C.POINTER(clk_image), C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]
+    lib.clk_server_submit.restype = C.c_int
+    lib.clk_server_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(C.c_double)]
+    lib.clk_server_wait.restype = C.c_int
+    lib.clk_server_drain.argtypes = [C.c_void_p, C.c_int32]
+    lib.clk_server_drain.restype = C.c_int
+    lib.clk_server_get_stats.argtypes = [C.c_void_p, C.POINTER(clk_server_stats)]
+    lib.clk_server_get_stats.restype = C.c_int
+    lib.clk_server_destroy.argtypes = [C.c_void_p]
+    lib.clk_server_destroy.restype = None
     lib.clk_supported.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32]
     lib.clk_supported.restype = C.c_int
     lib.clk_last_error_string.restype = C.c_char_p

@@ -228,3 +228,135 @@ def sobel(src, dst=None, stream=None, defines=None):
     dst = _out(src, dst, torch.float32)
     execute("sobel" + _suffix(src), {"dst": dst, "src": src}, defines=defines, stream=stream)
     return dst
+
+
+# ----------------------------------------------------------------- batch
+
+def op_separable(kernel: str, N, s=(0.0, 0.0, 0.0)) -> dict:
+    """A separable step: kernel base name without _2d/_3d, per-axis N and s."""
+    return {"kernel": kernel, "kind": L.OP_SEPARABLE, "N": list(N), "s": list(s)}
+
+
+def op_kernel(kernel: str, N=(1, 1, 1)) -> dict:
+    """A one-launch step (median_box / median_sphere with Nx, Ny, Nz; sobel)."""
+    return {"kernel": kernel, "kind": L.OP_KERNEL, "N": list(N)}
+
+
+def op_morphology(kernel: str, iterations: int = 1) -> dict:
+    """An erode/dilate step: the r=1 kernel applied `iterations` times."""
+    return {"kernel": kernel, "kind": L.OP_MORPHOLOGY, "iterations": int(iterations)}
+
+
+class Batch:
+    """A pipeline of steps over many images (clk_batch_*): one persistent
+    launch per step and pixel type over a tile work list, captured once as a
+    CUDA graph; results equal per-image plain calls."""
+
+    def __init__(self, ops, srcs, dsts, defines=None, stream=None):
+        lib = L.load()
+        if len(srcs) != len(dsts):
+            raise L.ClkError(L.BAD_ARG, "srcs and dsts differ in length")
+        self._keep = []
+        arr = (L.clk_op * len(ops))()
+        for k, o in enumerate(ops):
+            name = o["kernel"].encode()
+            self._keep.append(name)
+            n = list(o.get("N", (1, 1, 1))) + [1] * (3 - len(o.get("N", ())))
+            sg = [float(v) for v in o.get("s", (0.0, 0.0, 0.0))] + [0.0] * (3 - len(o.get("s", ())))
+            arr[k] = L.clk_op(name, o["kind"], (C.c_int32 * 3)(*n[:3]), (C.c_float * 3)(*sg[:3]),
+                              int(o.get("iterations", 1)))
+        si = (L.clk_image * len(srcs))(*[image_of(t) for t in srcs])
+        di = (L.clk_image * len(dsts))(*[image_of(t) for t in dsts])
+        darr, nd, self._dk = _defines(defines)
+        h = C.c_void_p()
+        L.check(lib.clk_batch_create(arr, len(ops), si, di, len(srcs), darr, nd, _stream(stream), C.byref(h)))
+        self._h = h
+        self._tensors = (list(srcs), list(dsts))  # keep the buffers alive
+
+    def run(self, stream=None):
+        L.check(L.load().clk_batch_run(self._h, _stream(stream)))
+
+    def run_plain(self, stream=None):
+        L.check(L.load().clk_batch_run_plain(self._h, _stream(stream)))
+
+    def run_per_kernel(self, stream=None):
+        L.check(L.load().clk_batch_run_per_kernel(self._h, _stream(stream)))
+
+    @property
+    def launches(self) -> int:
+        return int(L.load().clk_batch_launches(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.load().clk_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ops_array(ops, keep):
+    arr = (L.clk_op * len(ops))()
+    for k, o in enumerate(ops):
+        name = o["kernel"].encode()
+        keep.append(name)
+        n = list(o.get("N", (1, 1, 1))) + [1] * (3 - len(o.get("N", ())))
+        sg = [float(v) for v in o.get("s", (0.0, 0.0, 0.0))] + [0.0] * (3 - len(o.get("s", ())))
+        arr[k] = L.clk_op(name, o["kind"], (C.c_int32 * 3)(*n[:3]), (C.c_float * 3)(*sg[:3]),
+                          int(o.get("iterations", 1)))
+    return arr
+
+
+class Server:
+    """The served form (clk_server_*): requests are admitted in arrival
+    order as soon as a slot and HBM budget are free, run concurrently on
+    their own streams, and report their latency."""
+
+    def __init__(self, slots: int = 8, hbm_budget_bytes: int = 64 << 30):
+        h = C.c_void_p()
+        L.check(L.load().clk_server_create(int(slots), int(hbm_budget_bytes), C.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def submit(self, ops, src: torch.Tensor, dst: torch.Tensor, host_in=None, host_out=None) -> int:
+        keep = [src, dst, host_in, host_out]
+        arr = _ops_array(ops, keep)
+        si, di = image_of(src), image_of(dst)
+        t = C.c_uint64()
+        hin = host_in.data_ptr() if host_in is not None else None
+        hout = host_out.data_ptr() if host_out is not None else None
+        L.check(L.load().clk_server_submit(self._h, arr, len(ops), C.byref(si), C.byref(di), hin, hout,
+                                           C.byref(t)))
+        self._keep[t.value] = keep
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000) -> float:
+        lat = C.c_double()
+        st = L.load().clk_server_wait(self._h, ticket, int(timeout_ms), C.byref(lat))
+        if st != L.TIMEOUT:
+            self._keep.pop(ticket, None)
+        L.check(st)
+        return lat.value
+
+    def drain(self, timeout_ms: int = 600000):
+        L.check(L.load().clk_server_drain(self._h, int(timeout_ms)))
+
+    def stats(self) -> dict:
+        s = L.clk_server_stats()
+        L.check(L.load().clk_server_get_stats(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.load().clk_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

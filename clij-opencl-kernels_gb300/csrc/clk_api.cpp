@@ -8,6 +8,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -37,6 +38,7 @@ clk_status check_launch(const char* what) {
 }
 
 void count_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
+void uncount_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
 int dtype_size(int dt) {
   switch (dt) {
@@ -170,13 +172,32 @@ const KernelInfo* find_kernel(const char* name) {
   return nullptr;
 }
 
+volatile int* g_wait_flag_host = nullptr;
+int* g_wait_flag_dev = nullptr;
+
 clk_status device_ready() {
   static int count = -1;
+  static std::once_flag mapped;
   if (count < 0) {
     if (cudaGetDeviceCount(&count) != cudaSuccess) count = 0;
     cudaGetLastError();
   }
   if (count <= 0) return fail(CLK_NO_DEVICE, "no CUDA device available");
+  std::call_once(mapped, [] {
+    void* h = nullptr;
+    void* d = nullptr;
+    if (cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable) == cudaSuccess &&
+        cudaHostGetDevicePointer(&d, h, 0) == cudaSuccess) {
+      *(volatile int*)h = 0;
+      g_wait_flag_host = (volatile int*)h;
+      g_wait_flag_dev = (int*)d;
+    }
+    cudaGetLastError();
+  });
+  if (g_wait_flag_host && *g_wait_flag_host) {
+    *g_wait_flag_host = 0;
+    return fail(CLK_TIMEOUT, "a bounded wait for a staged tile ran out in an earlier launch; its output is incomplete");
+  }
   return CLK_OK;
 }
 
@@ -256,6 +277,10 @@ int slot_of(const KernelInfo& k, const char* nm) {
 }
 
 }  // namespace
+
+clk_status device_ready_public() { return device_ready(); }
+
+int* wait_flag_device() { return g_wait_flag_dev; }
 
 clk_status separable_plan(const char* kernel_name, const clk_image* dst_img, const clk_image* src_img,
                           const int32_t N[3], const float s[3], const clk_define* defines, size_t ndefines,

@@ -1,0 +1,117 @@
+// clk_batch.cuh - the batch engine's device-side descriptors and the
+// persistent kernels that walk a tile work list over many images.
+#pragma once
+#include "clk_fused_impl.cuh"
+#include "clk_median_impl.cuh"
+#include "clk_sep2_impl.cuh"
+
+namespace clk {
+namespace batch {
+
+// Tile bodies a work item can run (chosen per image on the host exactly as
+// the plain path chooses them, so batched results equal plain ones).
+enum Algo : int {
+  A_SEP2 = 1,         // register-window kernel, isotropic XY radius (clk_sep2_impl.cuh)
+  A_FUSED_EXACT = 2,  // generic fused kernel, reference order (clk_fused_impl.cuh)
+  A_FUSED_FAST = 3,   // generic fused kernel, FMA (float Gaussian)
+  A_MED27 = 4,        // median networks (clk_median_impl.cuh)
+  A_MED9 = 5,
+  A_MED33 = 6
+};
+
+struct WorkItem {
+  int img;
+  int bx, by, bz;
+};
+
+struct SepDesc {
+  const void* src;
+  void* dst;
+  int W, H, D, zchunk;
+  int dt, algo, rte;
+  sep2::Params p2;
+  fused::FusedTaps ft;
+};
+
+struct MedDesc {
+  const void* src;
+  void* dst;
+  int W, H, D, zchunk;
+  int dt, algo;
+};
+
+// SepOp (clk_internal.h) -> sep2's operation codes
+template <int OP> struct S2Op;
+template <> struct S2Op<SEP_MIN> { static constexpr int v = sep2::MIN; };
+template <> struct S2Op<SEP_MAX> { static constexpr int v = sep2::MAX; };
+template <> struct S2Op<SEP_MEAN> { static constexpr int v = sep2::MEAN; };
+template <> struct S2Op<SEP_GAUSS> { static constexpr int v = sep2::GAUSS; };
+
+constexpr int kmax_for(int R) { return R == 0 ? 63 : (2 * R + 1 <= 12 ? 12 : 24); }
+
+// One work item of a separable step; the pixel type picks the body.
+template <int OP, int R, class T>
+__device__ __forceinline__ void sep_item_t(const SepDesc& d, const WorkItem& it, unsigned char* smem) {
+  constexpr int KMAX = kmax_for(R);
+  const T* s = static_cast<const T*>(d.src);
+  T* o = static_cast<T*>(d.dst);
+  if constexpr (R >= 1 && sizeof(T) < 4 && OP != SEP_GAUSS) {
+    if (d.algo == A_SEP2) {
+      sep2::sep2_tile<T, T, S2Op<OP>::v, R>(s, o, d.W, d.H, d.D, d.zchunk, d.p2, it.bx, it.by, it.bz, smem);
+      return;
+    }
+  }
+  if constexpr (R >= 1 && sizeof(T) == 4 && OP == SEP_GAUSS) {
+    if (d.algo == A_SEP2) {
+      sep2::sep2_tile<T, T, sep2::GAUSS, R>(s, o, d.W, d.H, d.D, d.zchunk, d.p2, it.bx, it.by, it.bz, smem);
+      return;
+    }
+  }
+  if constexpr (sizeof(T) == 4 && OP == SEP_GAUSS) {
+    if (d.algo == A_FUSED_FAST) {
+      fused::fused_tile<T, T, OP, true, KMAX>(s, o, d.W, d.H, d.D, d.zchunk, d.ft, d.rte, it.bx, it.by, it.bz, smem);
+      return;
+    }
+  }
+  fused::fused_tile<T, T, OP, false, KMAX>(s, o, d.W, d.H, d.D, d.zchunk, d.ft, d.rte, it.bx, it.by, it.bz, smem);
+}
+
+// One persistent kernel per step and pixel type (a kernel's register
+// budget is that of its largest branch, so pixel types are not mixed).
+template <int OP, int R, class T>
+__global__ void __launch_bounds__(256) k_batch_sep(const WorkItem* __restrict__ items, int n,
+                                                   const SepDesc* __restrict__ descs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const WorkItem it = items[i];
+    sep_item_t<OP, R, T>(descs[it.img], it, smem);
+    __syncthreads();  // the next item reuses shared memory
+  }
+}
+
+template <class T> __device__ __forceinline__ void med_item_t(const MedDesc& d, const WorkItem& it) {
+  const T* s = static_cast<const T*>(d.src);
+  T* o = static_cast<T*>(d.dst);
+  if (d.algo == A_MED27) med::box27_tile<T>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+  else if (d.algo == A_MED33) med::sphere33_tile<T>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+  else med::box9_2d_tile<T>(s, o, d.W, d.H, it.bx, it.by);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_batch_median(const WorkItem* __restrict__ items, int n,
+                                                      const MedDesc* __restrict__ descs) {
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const WorkItem it = items[i];
+    med_item_t<T>(descs[it.img], it);
+  }
+}
+
+// host: the kernel for (op, R, pixel type); R = 0 is the generic-radius
+// variant.  nullptr if not instantiated.
+const void* batch_sep_kernel(int op, int R, int dt);
+template <int OP> const void* batch_sep_kernel_op(int R, int dt);  // one file per OP
+const void* batch_median_kernel(int dt);
+constexpr int kBatchRadii[] = {2, 3, 4, 5, 6};  // instantiated XY radii besides 0
+
+}  // namespace batch
+}  // namespace clk

@@ -64,6 +64,12 @@ struct MedianNbhd {
 clk_status fail(clk_status st, const char* fmt, ...);
 clk_status check_launch(const char* what);
 void count_launch(int n = 1);
+void uncount_launches(uint64_t n);  // launches recorded while capturing a graph
+clk_status device_ready_public();   // CLK_NO_DEVICE (with message) if no GPU
+// Device pointer of a host-mapped word that kernels set to 1 when one of
+// their bounded waits runs out (nullptr if it could not be mapped).  The next
+// entry-point call reports that as CLK_TIMEOUT and clears the word.
+int* wait_flag_device();
 
 int dtype_size(int dt);
 bool gauss_taps(int N, float s, SepTaps* t);  // false: window too large

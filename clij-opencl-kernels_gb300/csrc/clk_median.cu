@@ -35,7 +35,7 @@ Shape classify(bool sphere, const MedianNbhd& m, int ndim) {
 
 template <class T> clk_status launch(Shape sh, const Image& dst, const Image& src, cudaStream_t st) {
   const dim3 block(BX * BY);
-  const int tx = (src.w / 2 + BX - 1) / BX, ty = (src.h + BY - 1) / BY;
+  const int tx = ((src.w + 1) / 2 + BX - 1) / BX, ty = (src.h + BY - 1) / BY;
   if (sh == BOX9_2D) {
     k_median_box9_2d<T><<<dim3(tx, ty), block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h);
   } else {
@@ -61,7 +61,7 @@ template <class T> clk_status launch(Shape sh, const Image& dst, const Image& sr
 clk_status fast_median(bool sphere, const Image& dst, const Image& src, const MedianNbhd& m, cudaStream_t st) {
   const Shape sh = classify(sphere, m, src.ndim);
   if (sh == OTHER || src.dt != dst.dt) return CLK_UNSUPPORTED_DTYPE;
-  if (src.w % 2 != 0 || src.w != dst.w || src.h != dst.h || src.d != dst.d) return CLK_UNSUPPORTED_DTYPE;
+  if (src.w != dst.w || src.h != dst.h || src.d != dst.d) return CLK_UNSUPPORTED_DTYPE;
   const int align = dtype_size(src.dt) * 2;
   if (((uintptr_t)src.ptr | (uintptr_t)dst.ptr) % align != 0) return CLK_UNSUPPORTED_DTYPE;
   switch (src.dt) {

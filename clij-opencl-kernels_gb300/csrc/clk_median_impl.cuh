@@ -63,6 +63,12 @@ template <bool SG, int BYTES> struct Px16 {
   static __device__ __forceinline__ V lolo(V b) { return V{__byte_perm(b.v, 0, 0x1010)}; }
   static __device__ __forceinline__ V hihi(V b) { return V{__byte_perm(b.v, 0, 0x3232)}; }
   static __device__ __forceinline__ V hilo(V l, V b) { return V{__byte_perm(l.v, b.v, 0x5432)}; }
+  template <class T> static __device__ __forceinline__ V make(T a, T b) {
+    return V{(uint32_t)(uint16_t)(int16_t)a | ((uint32_t)(uint16_t)(int16_t)b << 16)};
+  }
+  template <class T> static __device__ __forceinline__ T lane(V v, int k) {
+    return (T)(int16_t)(uint16_t)(k ? v.v >> 16 : v.v);
+  }
 };
 template <> struct Px<uint16_t> : Px16<false, 2> {};
 template <> struct Px<int16_t> : Px16<true, 2> {};
@@ -80,13 +86,24 @@ template <> struct Px<float> {
   static __device__ __forceinline__ V lolo(V b) { return Keys{b.lo, b.lo}; }
   static __device__ __forceinline__ V hihi(V b) { return Keys{b.hi, b.hi}; }
   static __device__ __forceinline__ V hilo(V l, V b) { return Keys{l.hi, b.lo}; }
+  template <class T> static __device__ __forceinline__ V make(T a, T b) { return Keys{fkey(a), fkey(b)}; }
+  template <class T> static __device__ __forceinline__ T lane(V v, int k) { return fval(k ? v.hi : v.lo); }
 };
 
-template <class T> __device__ __forceinline__ typename Px<T>::V load_pair(const T* row, int x) {
-  return Px<T>::load(row, x);
+// Pixels (x, x+1) of a row (x even, x < W).  Rows of an even-width image
+// are pair-aligned and load/store as one word; for an odd width they take
+// two scalar accesses, x+1 clamped to the row on loads and skipped on stores.
+template <class T> __device__ __forceinline__ typename Px<T>::V load_pair(const T* row, int x, int W) {
+  if ((W & 1) == 0) return Px<T>::load(row, x);
+  return Px<T>::template make<T>(__ldg(row + x), __ldg(row + min(x + 1, W - 1)));
 }
-template <class T> __device__ __forceinline__ void store_pair(T* row, int x, typename Px<T>::V v) {
-  Px<T>::store(row, x, v);
+template <class T> __device__ __forceinline__ void store_pair(T* row, int x, int W, typename Px<T>::V v) {
+  if ((W & 1) == 0) {
+    Px<T>::store(row, x, v);
+  } else {
+    row[x] = Px<T>::template lane<T>(v, 0);
+    if (x + 1 < W) row[x + 1] = Px<T>::template lane<T>(v, 1);
+  }
 }
 
 // Values for the columns x-1, x, x+1 of the pair's outputs in one row:
@@ -95,9 +112,9 @@ template <class T> __device__ __forceinline__ void store_pair(T* row, int x, typ
 template <class T, class V = typename Px<T>::V>
 __device__ __forceinline__ void row_cols(const T* row, int x, int W, V& a, V& b, V& c, V* far_l = nullptr,
                                          V* far_r = nullptr) {
-  b = load_pair(row, x);
-  const V l = x >= 2 ? load_pair(row, x - 2) : Px<T>::lolo(b);
-  const V r = x + 2 < W ? load_pair(row, x + 2) : Px<T>::hihi(b);
+  b = load_pair(row, x, W);
+  const V l = x >= 2 ? load_pair(row, x - 2, W) : Px<T>::lolo(b);
+  const V r = x + 2 < W ? load_pair(row, x + 2, W) : Px<T>::hihi(b);
   a = Px<T>::hilo(l, b);
   c = Px<T>::hilo(b, r);
   if (far_l) *far_l = l;
@@ -178,8 +195,8 @@ __device__ __forceinline__ void box27_tile(const T* __restrict__ src, T* __restr
     block9<T>(src + (int64_t)clampi(zo + 1, D - 1) * plane, x, y, W, H, p1);
     block9<T>(src + (int64_t)clampi(zo + 2, D - 1) * plane, x, y, W, H, p2);
     merge_mid(p0, p1, m);
-    store_pair(dst + (int64_t)zo * plane + (int64_t)y * W, x, final27(m, pm1));
-    if (zo + 1 < z1) store_pair(dst + (int64_t)(zo + 1) * plane + (int64_t)y * W, x, final27(m, p2));
+    store_pair(dst + (int64_t)zo * plane + (int64_t)y * W, x, W, final27(m, pm1));
+    if (zo + 1 < z1) store_pair(dst + (int64_t)(zo + 1) * plane + (int64_t)y * W, x, W, final27(m, p2));
 #pragma unroll
     for (int k = 0; k < 9; ++k) pm1[k] = p1[k], p0[k] = p2[k];
   }
@@ -197,7 +214,7 @@ __device__ __forceinline__ void sphere33_tile(const T* __restrict__ src, T* __re
   if (x >= W || y >= H) return;
   const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
   const int64_t plane = (int64_t)W * H;
-  auto centre = [&](int z) { return load_pair(src + (int64_t)clampi(z, D - 1) * plane + (int64_t)y * W, x); };
+  auto centre = [&](int z) { return load_pair(src + (int64_t)clampi(z, D - 1) * plane + (int64_t)y * W, x, W); };
   V pm1[9], p0[9];
   block9<T>(src + (int64_t)clampi(z0 - 1, D - 1) * plane, x, y, W, H, pm1);
   block9<T>(src + (int64_t)z0 * plane, x, y, W, H, p0);
@@ -213,14 +230,14 @@ __device__ __forceinline__ void sphere33_tile(const T* __restrict__ src, T* __re
     {
       V a, b, c;
       row_cols<T>(pc + (int64_t)y * W, x, W, a, b, c, &w[27], &w[28]);
-      w[29] = load_pair(pc + (int64_t)clampi(y - 2, H - 1) * W, x);
-      w[30] = load_pair(pc + (int64_t)clampi(y + 2, H - 1) * W, x);
+      w[29] = load_pair(pc + (int64_t)clampi(y - 2, H - 1) * W, x, W);
+      w[30] = load_pair(pc + (int64_t)clampi(y + 2, H - 1) * W, x, W);
     }
     w[31] = cm2;
     w[32] = centre(zo + 2);
     const V cm1 = centre(zo - 1);
     net_sphere33_final_raw(w);
-    store_pair(dst + (int64_t)zo * plane + (int64_t)y * W, x, w[net_sphere33_final_out[0]]);
+    store_pair(dst + (int64_t)zo * plane + (int64_t)y * W, x, W, w[net_sphere33_final_out[0]]);
     cm2 = cm1;
 #pragma unroll
     for (int k = 0; k < 9; ++k) pm1[k] = p0[k], p0[k] = p1[k];
@@ -246,7 +263,7 @@ __device__ __forceinline__ void box9_2d_tile(const T* __restrict__ src, T* __res
     for (int k = 0; k < 3; ++k) w[3 * col + k] = t[net_sort3_out[k]];
   }
   net_med9_raw(w);
-  store_pair(dst + (int64_t)y * W, x, w[net_med9_out[0]]);
+  store_pair(dst + (int64_t)y * W, x, W, w[net_med9_out[0]]);
 }
 
 template <class T>

@@ -176,6 +176,99 @@ clk_status clk_morphology(const char* kernel_name, const clk_image* dst,
                           const clk_define* defines, size_t ndefines,
                           void* stream);
 
+/* ---------------------------------------------------------------------
+ * Batched form: the same pipeline of filters over many independent images
+ * of uneven shape and pixel type.  Each step runs as ONE persistent launch
+ * over a work list of tiles of all images (pixel type dispatched per tile),
+ * the pipeline is captured once as a CUDA graph, and the z-depth of a work
+ * item is picked by an autotuner whose choices persist in a JSON cache
+ * (env CLK_AUTOTUNE_CACHE, default $HOME/.cache/clk_gb300/autotune.json).
+ * Results equal per-image plain calls bit for bit.
+ * Replaces: the host loop that enqueues every kernel per image (CLIc /
+ *   pyclesperanto), which the reference leaves to its callers.
+ * ------------------------------------------------------------------- */
+typedef enum clk_op_kind {
+  CLK_OP_SEPARABLE = 0,  /* whole separable filter, as clk_separable       */
+  CLK_OP_KERNEL = 1,     /* one kernel launch, as clk_execute (median, sobel) */
+  CLK_OP_MORPHOLOGY = 2  /* r=1 kernel applied `iterations` times           */
+} clk_op_kind;
+
+/* One step, applied to every image.  kernel: a reference kernel name
+ * WITHOUT its _2d/_3d suffix (picked per image), e.g.
+ * "gaussian_blur_separable" (SEPARABLE: N[3], s[3] as clk_separable),
+ * "median_box" / "median_sphere" (KERNEL: N = Nx, Ny, Nz), "sobel",
+ * "erode_sphere" (MORPHOLOGY: iterations). */
+typedef struct clk_op {
+  const char* kernel;
+  int32_t kind; /* clk_op_kind */
+  int32_t N[3];
+  float s[3];
+  int32_t iterations;
+} clk_op;
+
+typedef struct clk_batch clk_batch;
+
+/* Plan a pipeline over images src[i] -> dst[i] (same extent; the steps'
+ * results and temporaries carry dst[i]'s pixel type).  Allocates the
+ * temporaries and work lists, autotunes (running the pipeline on the given
+ * images), and captures the CUDA graph.  The image buffers must stay valid
+ * until clk_batch_destroy. */
+clk_status clk_batch_create(const clk_op* ops, int32_t nops, const clk_image* src, const clk_image* dst,
+                            int32_t nimages, const clk_define* defines, size_t ndefines, void* stream,
+                            clk_batch** out);
+/* Run the pipeline (one graph launch) on the stream. */
+clk_status clk_batch_run(clk_batch* batch, void* stream);
+/* Run the same pipeline image by image with plain calls (no batching, no
+ * graph): the per-call baseline the batched form is measured against. */
+clk_status clk_batch_run_plain(clk_batch* batch, void* stream);
+/* The same pipeline as the reference's callers launch it: every kernel of
+ * every image by itself through clk_execute (a separable filter = one
+ * launch per axis with dst-typed temporaries, the orchestrator's pattern). */
+clk_status clk_batch_run_per_kernel(clk_batch* batch, void* stream);
+/* Kernel launches per clk_batch_run (nodes of the graph). */
+int32_t clk_batch_launches(const clk_batch* batch);
+void clk_batch_destroy(clk_batch* batch);
+
+/* ---------------------------------------------------------------------
+ * Served form: a request loop with continuous admission.  Each request is
+ * one image and a pipeline of steps (clk_op, suffix picked per image).  A
+ * scheduler thread admits queued requests in arrival order as soon as a
+ * slot (a CUDA stream) and HBM budget (the request's device temporaries)
+ * are free, so requests that arrive while others run start at once and
+ * their kernels overlap on the device.  Temporaries stay on the device;
+ * optional host buffers are copied in before and out after the pipeline on
+ * the request's stream.  Latency = submit -> completion of its last copy.
+ * Replaces: the per-request host loop of a serving application (not in the
+ * reference).
+ * ------------------------------------------------------------------- */
+typedef struct clk_server clk_server;
+
+typedef struct clk_server_stats {
+  uint64_t submitted, completed, failed;
+  int64_t bytes_in_use, bytes_peak;  /* admitted temporaries vs budget */
+  int32_t inflight, queued;
+  double p50_ms, p99_ms, mean_ms;    /* over completed requests */
+  double voxel_steps;                /* sum over completed of voxels x steps */
+  double busy_s;                     /* first submit -> last completion */
+} clk_server_stats;
+
+/* slots: concurrent requests (streams), 1..64; hbm_budget_bytes: limit on
+ * the admitted requests' temporaries (0 = no limit). */
+clk_status clk_server_create(int32_t slots, int64_t hbm_budget_bytes, clk_server** out);
+/* Queue a request; src/dst are device images (same extent), host_in /
+ * host_out optional host buffers of src's / dst's size (pinned memory makes
+ * the copies asynchronous).  CLK_BUSY if the queue is full; CLK_BAD_ARG if
+ * the request alone exceeds the budget. */
+clk_status clk_server_submit(clk_server* server, const clk_op* ops, int32_t nops, const clk_image* src,
+                             const clk_image* dst, const void* host_in, void* host_out, uint64_t* ticket);
+/* Wait (at most timeout_ms) for a request; CLK_TIMEOUT if it has not
+ * finished; its latency in ms. */
+clk_status clk_server_wait(clk_server* server, uint64_t ticket, int32_t timeout_ms, double* latency_ms);
+/* Wait (at most timeout_ms) until nothing is queued or in flight. */
+clk_status clk_server_drain(clk_server* server, int32_t timeout_ms);
+clk_status clk_server_get_stats(clk_server* server, clk_server_stats* out);
+void clk_server_destroy(clk_server* server);
+
 /* Is kernel_name available for this (src, dst) pixel-type pair and ndim?
  * Returns 1 if yes, 0 if no. */
 int clk_supported(const char* kernel_name, int32_t src_dtype,

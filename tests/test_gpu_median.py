@@ -38,7 +38,7 @@ CASES = [("median_box_3d", {"Nx": 3, "Ny": 3, "Nz": 3}), ("median_sphere_3d", {"
 @pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.int8, np.float32])
 def test_network_median_3d(clk, oracle, kernel, params, dt):
     rng = np.random.default_rng(23)
-    for shp in ((21, 37, 130), (1, 5, 64), (2, 1, 2), (7, 64, 2), (33, 16, 66)):
+    for shp in ((21, 37, 130), (1, 5, 64), (2, 1, 2), (7, 64, 2), (33, 16, 66), (9, 13, 67), (4, 6, 1), (3, 5, 3)):
         for lo, hi in ((None, None), (0, 3)):  # full range, and many ties
             a = random_image(rng, shp, dt)
             if lo is not None:
@@ -51,7 +51,7 @@ def test_network_median_3d(clk, oracle, kernel, params, dt):
 @pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.int8])
 def test_network_median_2d(clk, oracle, dt):
     rng = np.random.default_rng(24)
-    for shp in ((37, 130), (1, 64), (5, 2)):
+    for shp in ((37, 130), (1, 64), (5, 2), (31, 67), (7, 1)):
         a = random_image(rng, shp, dt)
         want = oracle.execute("median_box_2d", a, dt, [3, 3])
         assert np.array_equal(run(clk, "median_box_2d", a, {"Nx": 3, "Ny": 3}), want)

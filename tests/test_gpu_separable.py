@@ -40,7 +40,7 @@ def close(got, val, scale):
 @pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.int8])
 def test_integer_isotropic_radii(clk, oracle, kernel, dt):
     rng = np.random.default_rng(31)
-    for shp in ((19, 70, 130), (3, 33, 64), (1, 40, 66), (40, 8, 10)):
+    for shp in ((19, 70, 130), (3, 33, 64), (1, 40, 66), (40, 8, 10), (6, 29, 67), (2, 9, 1)):
         a = random_image(rng, shp, dt)
         for R in range(1, 9):
             for rz in (0, 1, R):
@@ -53,7 +53,7 @@ def test_integer_isotropic_radii(clk, oracle, kernel, dt):
 @pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.float32])
 def test_gaussian_to_float_isotropic(clk, oracle, dt):
     rng = np.random.default_rng(32)
-    for shp in ((17, 70, 130), (2, 35, 64)):
+    for shp in ((17, 70, 130), (2, 35, 64), (5, 23, 45)):
         a = random_image(rng, shp, dt)
         for R in (1, 3, 6, 9, 12):
             sig = R / 3.0
