@@ -202,8 +202,8 @@ def batch_images(n=512, seed=3, device="cuda"):
 
 
 def run_batch(args):
-    """BASELINE config 3: the top-hat chain over the uneven batch, batched
-    (one graph launch) against per-image plain calls, same results."""
+    """Top-hat chain over 512 uneven images, batched (one graph launch)
+    against per-image plain calls, same results."""
     import torch
 
     import clk
@@ -257,7 +257,7 @@ def run_batch(args):
         "unit": "Gvoxel/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
         "ms_per_step": round(ms_b, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u8/u16/f32 pixels, same type out", "data": "synthetic: seeded blob images, intensities scaled to type",
-        "config": {"workload": "config 3: 512 images (half 2-D XY in [64,1024], half 3-D XY in [64,512] x Z in "
+        "config": {"workload": "batched top-hat: 512 images (half 2-D XY in [64,1024], half 3-D XY in [64,512] x Z in "
                                "[16,128]), top-hat chain gaussian s=2 -> minimum r=4 -> maximum r=4 -> median_box r=1",
                    "images": len(imgs), "u8": n_u8, "u16": n_u16, "f32": len(imgs) - n_u8 - n_u16,
                    "voxels_per_step": vox, "l2": "working set far larger than L2"},
@@ -299,8 +299,8 @@ def serve_pipeline(clk, rng):
 
 
 def run_serve(args):
-    """BASELINE config 4: Poisson arrivals at 200 / 1000 / 5000 req/s, each
-    request one stack from the config-3 size and type distribution and a
+    """Served pipelines: Poisson arrivals at 200 / 1000 / 5000 req/s, each
+    request one stack from the batched workload's size and type mix and a
     random 1-4 step pipeline, served with continuous admission (16 slots,
     64 GiB budget) against the same arrivals served one at a time."""
     import numpy as np
@@ -342,15 +342,85 @@ def run_serve(args):
         results.append(row)
     top = results[-1]
     line = {
-        "metric": "served p99 latency and Gvoxel/s (Poisson arrivals, config-3 stacks, 1-4 step pipelines)",
+        "metric": "served p99 latency and Gvoxel/s (Poisson arrivals, uneven u8/u16/f32 stacks, 1-4 step pipelines)",
         "value": top["served"]["p99_ms"], "unit": "ms (p99 at 5000 req/s)", "n_gpus": 1, "steps": len(results),
         "warmup": 1, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "u8/u16/f32 pixels, same type out", "data": "synthetic: 96 seeded blob stacks, random pipelines",
-        "config": {"workload": "config 4: continuous admission, 16 slots, 64 GiB budget for temporaries; serial "
+        "config": {"workload": "served pipelines: continuous admission, 16 slots, 64 GiB budget for temporaries; serial "
                                "= the same arrivals through 1 slot", "duration_s_per_rate": duration},
         "rates": results,
     }
     print(json.dumps(line))
+
+
+LARGE_SHAPE = (400, 2048, 2048)  # (z, y, x): 6.71 GB of float32
+
+
+def run_large(args):
+    """Large-halo filters on one 2048x2048x400 float32 stack (blobs plus
+    N(0, 20) noise): gaussian sigma (10,10,5) (N = 61,61,31), maximum r
+    (15,15,7) and median_sphere r=2, each its own call, f32 -> f32."""
+    import torch
+
+    import clk
+    from clk import synth
+
+    torch.cuda.set_device(0)
+    peak, peak_kind = hbm_peak()
+    img = synth.blobs(LARGE_SHAPE, N_BLOBS, seed=SEED + 5, dtype=torch.float32, poisson=False, noise_sigma=20.0)
+    V = img.numel()
+    out = torch.empty_like(img)
+    stream = torch.cuda.current_stream()
+    spec = [
+        ("gaussian_blur s(10,10,5)", lambda: clk.separable("gaussian_blur_separable_3d", img, out, (61, 61, 31),
+                                                           (10.0, 10.0, 5.0), stream=stream)),
+        ("maximum_box r(15,15,7)", lambda: clk.separable("maximum_separable_3d", img, out, (31, 31, 15),
+                                                         (15.0, 15.0, 7.0), stream=stream)),
+        ("median_sphere r2", lambda: clk.execute("median_sphere_3d", {"src": img, "dst": out, "Nx": 5, "Ny": 5,
+                                                                       "Nz": 5}, stream=stream)),
+    ]
+    for _ in range(max(3, args.warmup)):
+        for _, fn in spec:
+            fn()
+    torch.cuda.synchronize()
+    ev = {n: [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)] for n, _ in spec}
+    t_begin, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = clk.launch_count()
+    with Clocks(0) as clocks:
+        torch.cuda.synchronize()
+        t_begin.record(stream)
+        for k in range(args.steps):
+            for n, fn in spec:
+                ev[n][k][0].record(stream)
+                fn()
+                ev[n][k][1].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    launches = clk.launch_count() - launches0
+    total_ms = t_begin.elapsed_time(t_end)
+    per = {}
+    for n, _ in spec:
+        ms = statistics.mean(a.elapsed_time(b) for a, b in ev[n])
+        per[n] = {"ms": round(ms, 3), "gvox_s": round(V / (ms * 1e-3) / 1e9, 2),
+                  "hbm_frac": round(V * 8 / (ms * 1e-3) / 1e9 / peak, 4), "bytes_per_voxel": 8}
+    dom = max(per, key=lambda n: per[n]["ms"])
+    dom_gbs = V * 8 / (per[dom]["ms"] * 1e-3) / 1e9
+    line = {
+        "metric": "Gvoxel/s (large-halo filters, 2048x2048x400 f32)", "value": round(
+            V * len(spec) * args.steps / (total_ms * 1e-3) / 1e9, 3), "unit": "Gvoxel/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(total_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded blob stack plus N(0,20) noise, float32",
+        "config": {"workload": "large-halo filters on 2048x2048x400 float32, each its own call", "voxels": V,
+                   "l2": "inputs larger than L2 (6.7 GB); no flush"},
+        "per_filter": per,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(dom_gbs, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(dom_gbs / peak, 4), "peak_kind": peak_kind, "traffic": None},
+        "gpu_launches": launches, "clocks": clocks.result,
+    }
+    print(json.dumps(line))
+    return 0
 
 
 def cpu_baseline(a_np, mask_np):
@@ -391,13 +461,19 @@ def main():
     ap.add_argument("--full-sample", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="suite", choices=["suite", "batch", "serve"],
-                    help="suite: config 2 (default); batch: config 3; serve: config 4")
+    ap.add_argument("--shape", default="", help="suite stack as z,y,x (default 256,1024,1024)")
+    ap.add_argument("--filters", default="", help="regex selecting suite filters by name")
+    ap.add_argument("--workload", default="suite", choices=["suite", "batch", "serve", "large"],
+                    help="suite: plain filter suite on 1024x1024x256 u16 (default); batch: top-hat chain over 512 uneven "
+                         "images; serve: Poisson-arrival requests; large: large-halo f32 "
+                         "filters on 2048x2048x400")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "large":
+        return run_large(args)
     if args.workload == "serve":
         return run_serve(args)
 
@@ -414,13 +490,20 @@ def main():
     dev = torch.device("cuda", local)
     peak, peak_kind = hbm_peak()
 
-    img = synth.blobs(SHAPE, N_BLOBS, seed=SEED + rank, dtype=torch.uint16, device=dev)
+    shape = SHAPE
+    if args.shape:  # a smaller stack of the same data density (profiling captures)
+        shape = tuple(int(v) for v in args.shape.split(","))
+    n_blobs = max(1, int(N_BLOBS * shape[0] * shape[1] * shape[2] / (SHAPE[0] * SHAPE[1] * SHAPE[2])))
+    img = synth.blobs(shape, n_blobs, seed=SEED + rank, dtype=torch.uint16, device=dev)
     mask = synth.mask_of(img, 400.0)
     V = img.numel()
     spec = suite_spec()
+    if args.filters:
+        import re
+        spec = [s for s in spec if re.search(args.filters, s[0])]
     outs = {}
     for name, kind, kernel, params, srcn, ddt, bpv in spec:
-        outs[name] = torch.empty(SHAPE, dtype=clk.torch_dtype(ddt), device=dev)
+        outs[name] = torch.empty(shape, dtype=clk.torch_dtype(ddt), device=dev)
     tmp_mask = torch.empty_like(mask)
     stream = torch.cuda.current_stream()
 
@@ -481,7 +564,7 @@ def main():
     if not args.no_e2e:
         h_img = img.cpu().pin_memory()
         h_mask = mask.cpu().pin_memory()
-        h_out = {n: torch.empty(SHAPE, dtype=o.dtype).pin_memory() for n, o in outs.items()}
+        h_out = {n: torch.empty(shape, dtype=o.dtype).pin_memory() for n, o in outs.items()}
         d_img, d_mask = torch.empty_like(img), torch.empty_like(mask)
 
         def e2e_step():
@@ -518,8 +601,8 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u16 in (u8 mask); u16/f32/u8 out; f32 arithmetic",
             "data": "synthetic: seeded blob stack (background 100, 20k Gaussian blobs, Poisson), mask = img > 400",
-            "config": {"workload": "plain filter suite, 1024x1024x256 uint16 stack + uint8 mask, each filter "
-                                   "run separately", "voxels": V, "filters": [s[0] for s in spec],
+            "config": {"workload": f"plain filter suite, {shape[2]}x{shape[1]}x{shape[0]} uint16 stack + uint8 "
+                                   "mask, each filter run separately", "voxels": V, "filters": [s[0] for s in spec],
                        "l2": "inputs larger than L2 (512 MiB stack, 256 MiB mask); no flush"},
             "per_filter": per,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(dom_gbs, 1), "peak": peak,

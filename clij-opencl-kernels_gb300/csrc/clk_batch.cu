@@ -93,7 +93,6 @@ size_t sep2_smem(int op, int R, int dt, int cz) {
   return 0;
 }
 
-uint64_t recip40(int n) { return (((uint64_t)1 << 40) + (uint64_t)n - 1) / (uint64_t)n; }
 
 // ---------------------------------------------------------------- tuning cache
 class TuneCache {
@@ -310,8 +309,8 @@ ImgStep plan_sep(clk_batch* b, int s, int i, SepDesc* d) {
       if (!batch_radius(R) || sep2_smem(opn, R, in.dt, cz) > 220 * 1024) return h;  // plain call keeps parity
       d->algo = A_SEP2;
       d->p2.cz = cz;
-      d->p2.mx = recip40(2 * R + 1);
-      d->p2.mz = recip40(2 * cz + 1);
+      d->p2.mx = sep2::recip32(2 * R + 1);
+      d->p2.mz = sep2::recip32(2 * cz + 1);
       if (s2_gauss) {
         for (int a = 0; a < 3; ++a) {
           const int c = ft.c[a];

@@ -92,9 +92,15 @@ __global__ void __launch_bounds__(256) k_batch_sep(const WorkItem* __restrict__ 
 template <class T> __device__ __forceinline__ void med_item_t(const MedDesc& d, const WorkItem& it) {
   const T* s = static_cast<const T*>(d.src);
   T* o = static_cast<T*>(d.dst);
-  if (d.algo == A_MED27) med::box27_tile<T>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
-  else if (d.algo == A_MED33) med::sphere33_tile<T>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
-  else med::box9_2d_tile<T>(s, o, d.W, d.H, it.bx, it.by);
+  if (d.W & 1) {
+    if (d.algo == A_MED27) med::box27_tile<T, true>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+    else if (d.algo == A_MED33) med::sphere33_tile<T, true>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+    else med::box9_2d_tile<T, true>(s, o, d.W, d.H, it.bx, it.by);
+  } else {
+    if (d.algo == A_MED27) med::box27_tile<T, false>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+    else if (d.algo == A_MED33) med::sphere33_tile<T, false>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+    else med::box9_2d_tile<T, false>(s, o, d.W, d.H, it.bx, it.by);
+  }
 }
 
 template <class T>

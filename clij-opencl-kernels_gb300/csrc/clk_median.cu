@@ -33,11 +33,11 @@ Shape classify(bool sphere, const MedianNbhd& m, int ndim) {
   return OTHER;
 }
 
-template <class T> clk_status launch(Shape sh, const Image& dst, const Image& src, cudaStream_t st) {
+template <class T, bool ODD> clk_status launch(Shape sh, const Image& dst, const Image& src, cudaStream_t st) {
   const dim3 block(BX * BY);
   const int tx = ((src.w + 1) / 2 + BX - 1) / BX, ty = (src.h + BY - 1) / BY;
   if (sh == BOX9_2D) {
-    k_median_box9_2d<T><<<dim3(tx, ty), block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h);
+    k_median_box9_2d<T, ODD><<<dim3(tx, ty), block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h);
   } else {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -48,9 +48,9 @@ template <class T> clk_status launch(Shape sh, const Image& dst, const Image& sr
     zchunk += zchunk & 1;  // box: outputs come in z pairs
     const dim3 grid(tx, ty, (src.d + zchunk - 1) / zchunk);
     if (sh == BOX27)
-      k_median_box27<T><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);
+      k_median_box27<T, ODD><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);
     else
-      k_median_sphere33<T><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);
+      k_median_sphere33<T, ODD><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);
   }
   count_launch();
   return check_launch("median (networks)");
@@ -64,12 +64,13 @@ clk_status fast_median(bool sphere, const Image& dst, const Image& src, const Me
   if (src.w != dst.w || src.h != dst.h || src.d != dst.d) return CLK_UNSUPPORTED_DTYPE;
   const int align = dtype_size(src.dt) * 2;
   if (((uintptr_t)src.ptr | (uintptr_t)dst.ptr) % align != 0) return CLK_UNSUPPORTED_DTYPE;
+  const bool odd = src.w & 1;
   switch (src.dt) {
-    case CLK_U16: return launch<uint16_t>(sh, dst, src, st);
-    case CLK_I16: return launch<int16_t>(sh, dst, src, st);
-    case CLK_U8: return launch<uint8_t>(sh, dst, src, st);
-    case CLK_I8: return launch<int8_t>(sh, dst, src, st);
-    case CLK_F32: return launch<float>(sh, dst, src, st);
+    case CLK_U16: return odd ? launch<uint16_t, true>(sh, dst, src, st) : launch<uint16_t, false>(sh, dst, src, st);
+    case CLK_I16: return odd ? launch<int16_t, true>(sh, dst, src, st) : launch<int16_t, false>(sh, dst, src, st);
+    case CLK_U8: return odd ? launch<uint8_t, true>(sh, dst, src, st) : launch<uint8_t, false>(sh, dst, src, st);
+    case CLK_I8: return odd ? launch<int8_t, true>(sh, dst, src, st) : launch<int8_t, false>(sh, dst, src, st);
+    case CLK_F32: return odd ? launch<float, true>(sh, dst, src, st) : launch<float, false>(sh, dst, src, st);
   }
   return CLK_UNSUPPORTED_DTYPE;
 }

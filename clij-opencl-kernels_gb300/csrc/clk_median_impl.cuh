@@ -52,7 +52,10 @@ template <bool SG, int BYTES> struct Px16 {
       v.v = __ldg(reinterpret_cast<const uint32_t*>(row) + x / 2);
     } else {
       const uint32_t w = __ldg(reinterpret_cast<const uint16_t*>(row) + x / 2);
-      v.v = SG ? __byte_perm(w, 0, 0x9180) : __byte_perm(w, 0, 0x4140);
+      if constexpr (SG)  // sign-extend each byte to its 16-bit lane
+        v.v = ((uint32_t)((int)(w << 24) >> 24) & 0xFFFFu) | ((uint32_t)((int)(w << 16) >> 24) << 16);
+      else
+        v.v = __byte_perm(w, 0, 0x4140);
     }
     return v;
   }
@@ -90,15 +93,18 @@ template <> struct Px<float> {
   template <class T> static __device__ __forceinline__ T lane(V v, int k) { return fval(k ? v.hi : v.lo); }
 };
 
-// Pixels (x, x+1) of a row (x even, x < W).  Rows of an even-width image
-// are pair-aligned and load/store as one word; for an odd width they take
-// two scalar accesses, x+1 clamped to the row on loads and skipped on stores.
-template <class T> __device__ __forceinline__ typename Px<T>::V load_pair(const T* row, int x, int W) {
-  if ((W & 1) == 0) return Px<T>::load(row, x);
-  return Px<T>::template make<T>(__ldg(row + x), __ldg(row + min(x + 1, W - 1)));
+// Pixels (x, x+1) of a row (x even, x < W).  ODD is the parity of W: rows
+// of an even-width image are pair-aligned and load/store as one word; for an
+// odd width they take two scalar accesses, x+1 clamped to the row on loads
+// and skipped on stores.  (The parity is a template argument so that the
+// even-width kernels carry no scalar path and no extra registers.)
+template <class T, bool ODD> __device__ __forceinline__ typename Px<T>::V load_pair(const T* row, int x, int W) {
+  if constexpr (!ODD) return Px<T>::load(row, x);
+  else return Px<T>::template make<T>(__ldg(row + x), __ldg(row + min(x + 1, W - 1)));
 }
-template <class T> __device__ __forceinline__ void store_pair(T* row, int x, int W, typename Px<T>::V v) {
-  if ((W & 1) == 0) {
+template <class T, bool ODD>
+__device__ __forceinline__ void store_pair(T* row, int x, int W, typename Px<T>::V v) {
+  if constexpr (!ODD) {
     Px<T>::store(row, x, v);
   } else {
     row[x] = Px<T>::template lane<T>(v, 0);
@@ -109,12 +115,12 @@ template <class T> __device__ __forceinline__ void store_pair(T* row, int x, int
 // Values for the columns x-1, x, x+1 of the pair's outputs in one row:
 // a = (x-1, x), b = (x, x+1), c = (x+1, x+2), clamped at the row ends; far_l
 // = (x-2, x-1) and far_r = (x+2, x+3), also clamped.
-template <class T, class V = typename Px<T>::V>
+template <class T, bool ODD, class V = typename Px<T>::V>
 __device__ __forceinline__ void row_cols(const T* row, int x, int W, V& a, V& b, V& c, V* far_l = nullptr,
                                          V* far_r = nullptr) {
-  b = load_pair(row, x, W);
-  const V l = x >= 2 ? load_pair(row, x - 2, W) : Px<T>::lolo(b);
-  const V r = x + 2 < W ? load_pair(row, x + 2, W) : Px<T>::hihi(b);
+  b = load_pair<T, ODD>(row, x, W);
+  const V l = x >= 2 ? load_pair<T, ODD>(row, x - 2, W) : Px<T>::lolo(b);
+  const V r = x + 2 < W ? load_pair<T, ODD>(row, x + 2, W) : Px<T>::hihi(b);
   a = Px<T>::hilo(l, b);
   c = Px<T>::hilo(b, r);
   if (far_l) *far_l = l;
@@ -128,13 +134,13 @@ template <class V, int N, int M> __device__ __forceinline__ void pick(const V (&
 
 // Sorted 9 of the 3x3 block of plane (rows y-1..y+1, columns x-1..x+1) for
 // both lanes, plus optionally the extra values the sphere needs.
-template <class T, class V>
+template <class T, bool ODD, class V>
 __device__ __forceinline__ void block9(const T* plane, int x, int y, int W, int H, V (&p)[9]) {
   V w[9];
 #pragma unroll
   for (int dy = -1; dy <= 1; ++dy) {
     const T* row = plane + (int64_t)clampi(y + dy, H - 1) * W;
-    row_cols<T>(row, x, W, w[dy + 1], w[dy + 4], w[dy + 7]);
+    row_cols<T, ODD>(row, x, W, w[dy + 1], w[dy + 4], w[dy + 7]);
   }
   {
     V t[3] = {w[0], w[1], w[2]};
@@ -177,8 +183,8 @@ constexpr int BX = 32;  // threads (= pairs) per row of a tile
 constexpr int BY = 8;   // rows per tile
 
 // Tile bodies: tile (bx, by) x z-chunk bz, threads of a 256-thread CTA map to
-// BX pairs x BY rows.
-template <class T>
+// BX pairs x BY rows.  ODD must equal W & 1.
+template <class T, bool ODD>
 __device__ __forceinline__ void box27_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int D,
                                            int zchunk, int bx, int by, int bz) {
   using V = typename Px<T>::V;
@@ -188,15 +194,15 @@ __device__ __forceinline__ void box27_tile(const T* __restrict__ src, T* __restr
   const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
   const int64_t plane = (int64_t)W * H;
   V pm1[9], p0[9];
-  block9<T>(src + (int64_t)clampi(z0 - 1, D - 1) * plane, x, y, W, H, pm1);
-  block9<T>(src + (int64_t)z0 * plane, x, y, W, H, p0);
+  block9<T, ODD>(src + (int64_t)clampi(z0 - 1, D - 1) * plane, x, y, W, H, pm1);
+  block9<T, ODD>(src + (int64_t)z0 * plane, x, y, W, H, p0);
   for (int zo = z0; zo < z1; zo += 2) {
     V p1[9], p2[9], m[10];
-    block9<T>(src + (int64_t)clampi(zo + 1, D - 1) * plane, x, y, W, H, p1);
-    block9<T>(src + (int64_t)clampi(zo + 2, D - 1) * plane, x, y, W, H, p2);
+    block9<T, ODD>(src + (int64_t)clampi(zo + 1, D - 1) * plane, x, y, W, H, p1);
+    block9<T, ODD>(src + (int64_t)clampi(zo + 2, D - 1) * plane, x, y, W, H, p2);
     merge_mid(p0, p1, m);
-    store_pair(dst + (int64_t)zo * plane + (int64_t)y * W, x, W, final27(m, pm1));
-    if (zo + 1 < z1) store_pair(dst + (int64_t)(zo + 1) * plane + (int64_t)y * W, x, W, final27(m, p2));
+    store_pair<T, ODD>(dst + (int64_t)zo * plane + (int64_t)y * W, x, W, final27(m, pm1));
+    if (zo + 1 < z1) store_pair<T, ODD>(dst + (int64_t)(zo + 1) * plane + (int64_t)y * W, x, W, final27(m, p2));
 #pragma unroll
     for (int k = 0; k < 9; ++k) pm1[k] = p1[k], p0[k] = p2[k];
   }
@@ -205,7 +211,7 @@ __device__ __forceinline__ void box27_tile(const T* __restrict__ src, T* __restr
 // median_sphere_3d with Nx = Ny = Nz = 5: per output the 3x3 blocks of
 // planes z-1, z, z+1, the four voxels at distance 2 in plane z and the two
 // at distance 2 along z (33 = 9 + 9 + 9 + 4 + 2).
-template <class T>
+template <class T, bool ODD>
 __device__ __forceinline__ void sphere33_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int D,
                                               int zchunk, int bx, int by, int bz) {
   using V = typename Px<T>::V;
@@ -214,30 +220,32 @@ __device__ __forceinline__ void sphere33_tile(const T* __restrict__ src, T* __re
   if (x >= W || y >= H) return;
   const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
   const int64_t plane = (int64_t)W * H;
-  auto centre = [&](int z) { return load_pair(src + (int64_t)clampi(z, D - 1) * plane + (int64_t)y * W, x, W); };
+  auto centre = [&](int z) {
+    return load_pair<T, ODD>(src + (int64_t)clampi(z, D - 1) * plane + (int64_t)y * W, x, W);
+  };
   V pm1[9], p0[9];
-  block9<T>(src + (int64_t)clampi(z0 - 1, D - 1) * plane, x, y, W, H, pm1);
-  block9<T>(src + (int64_t)z0 * plane, x, y, W, H, p0);
+  block9<T, ODD>(src + (int64_t)clampi(z0 - 1, D - 1) * plane, x, y, W, H, pm1);
+  block9<T, ODD>(src + (int64_t)z0 * plane, x, y, W, H, p0);
   V cm2 = centre(z0 - 2);
   for (int zo = z0; zo < z1; ++zo) {
     V p1[9];
     const T* pz = src + (int64_t)clampi(zo + 1, D - 1) * plane;
-    block9<T>(pz, x, y, W, H, p1);
+    block9<T, ODD>(pz, x, y, W, H, p1);
     const T* pc = src + (int64_t)zo * plane;
     V w[33];
 #pragma unroll
     for (int k = 0; k < 9; ++k) w[k] = pm1[k], w[9 + k] = p1[k], w[18 + k] = p0[k];
     {
       V a, b, c;
-      row_cols<T>(pc + (int64_t)y * W, x, W, a, b, c, &w[27], &w[28]);
-      w[29] = load_pair(pc + (int64_t)clampi(y - 2, H - 1) * W, x, W);
-      w[30] = load_pair(pc + (int64_t)clampi(y + 2, H - 1) * W, x, W);
+      row_cols<T, ODD>(pc + (int64_t)y * W, x, W, a, b, c, &w[27], &w[28]);
+      w[29] = load_pair<T, ODD>(pc + (int64_t)clampi(y - 2, H - 1) * W, x, W);
+      w[30] = load_pair<T, ODD>(pc + (int64_t)clampi(y + 2, H - 1) * W, x, W);
     }
     w[31] = cm2;
     w[32] = centre(zo + 2);
     const V cm1 = centre(zo - 1);
     net_sphere33_final_raw(w);
-    store_pair(dst + (int64_t)zo * plane + (int64_t)y * W, x, W, w[net_sphere33_final_out[0]]);
+    store_pair<T, ODD>(dst + (int64_t)zo * plane + (int64_t)y * W, x, W, w[net_sphere33_final_out[0]]);
     cm2 = cm1;
 #pragma unroll
     for (int k = 0; k < 9; ++k) pm1[k] = p0[k], p0[k] = p1[k];
@@ -245,7 +253,7 @@ __device__ __forceinline__ void sphere33_tile(const T* __restrict__ src, T* __re
 }
 
 // median_box_2d 3x3.
-template <class T>
+template <class T, bool ODD>
 __device__ __forceinline__ void box9_2d_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int bx,
                                              int by) {
   using V = typename Px<T>::V;
@@ -254,7 +262,7 @@ __device__ __forceinline__ void box9_2d_tile(const T* __restrict__ src, T* __res
   if (x >= W || y >= H) return;
   V w[9];
 #pragma unroll
-  for (int dy = -1; dy <= 1; ++dy) row_cols<T>(src + (int64_t)clampi(y + dy, H - 1) * W, x, W, w[dy + 1], w[dy + 4], w[dy + 7]);
+  for (int dy = -1; dy <= 1; ++dy) row_cols<T, ODD>(src + (int64_t)clampi(y + dy, H - 1) * W, x, W, w[dy + 1], w[dy + 4], w[dy + 7]);
 #pragma unroll
   for (int col = 0; col < 3; ++col) {
     V t[3] = {w[3 * col], w[3 * col + 1], w[3 * col + 2]};
@@ -263,23 +271,27 @@ __device__ __forceinline__ void box9_2d_tile(const T* __restrict__ src, T* __res
     for (int k = 0; k < 3; ++k) w[3 * col + k] = t[net_sort3_out[k]];
   }
   net_med9_raw(w);
-  store_pair(dst + (int64_t)y * W, x, W, w[net_med9_out[0]]);
+  store_pair<T, ODD>(dst + (int64_t)y * W, x, W, w[net_med9_out[0]]);
 }
 
-template <class T>
+template <class T, bool ODD>
 __global__ void __launch_bounds__(BX * BY) k_median_box27(const T* __restrict__ src, T* __restrict__ dst, int W,
                                                           int H, int D, int zchunk) {
-  box27_tile<T>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
+  box27_tile<T, ODD>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
 }
-template <class T>
-__global__ void __launch_bounds__(BX * BY) k_median_sphere33(const T* __restrict__ src, T* __restrict__ dst, int W,
+// 16-bit pixels fit the sphere network in 64 registers without spilling:
+// four CTAs per SM instead of three
+template <class T> constexpr int sphere_min_ctas() { return sizeof(T) == 2 ? 4 : sizeof(T) == 1 ? 3 : 2; }
+
+template <class T, bool ODD>
+__global__ void __launch_bounds__(BX * BY, sphere_min_ctas<T>()) k_median_sphere33(const T* __restrict__ src, T* __restrict__ dst, int W,
                                                              int H, int D, int zchunk) {
-  sphere33_tile<T>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
+  sphere33_tile<T, ODD>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
 }
-template <class T>
+template <class T, bool ODD>
 __global__ void __launch_bounds__(BX * BY) k_median_box9_2d(const T* __restrict__ src, T* __restrict__ dst, int W,
                                                             int H) {
-  box9_2d_tile<T>(src, dst, W, H, blockIdx.x, blockIdx.y);
+  box9_2d_tile<T, ODD>(src, dst, W, H, blockIdx.x, blockIdx.y);
 }
 
 }  // namespace med

@@ -105,14 +105,34 @@ __global__ void __launch_bounds__(MT)
   uint4* dst4 = reinterpret_cast<uint4*>(dst);
   const int hx = ITER, hy = ITER;  // halo of the staged input around the output tile
 
-  auto load_plane = [&](int zv, int slot) {
+  // Input planes are staged strictly in z order.  The next one is always in
+  // flight in registers (pf) while the current planes are processed;
+  // load_plane(zv, slot) stores plane zv (the prefetched one) as masks and
+  // starts fetching zv + 1 if it will be needed.
+  constexpr int NS = G::IY * G::IX, PERM = (NS + MT - 1) / MT;
+  const int last_in = z1 - 1 + ITER;
+  uint4 pf[PERM];
+  auto fetch = [&](int zv) {
     const int zc = clampi(zv, Dz - 1);
-    for (int i = tid; i < G::IY * G::IX; i += MT) {
-      const int r = i / G::IX, q = i - r * G::IX;
-      const int gy = clampi(y0 - hy + r, H - 1), gq = clampi(xc0 - hx + q, nxc - 1);
-      in[slot][i] = nzmask(__ldg(src4 + ((int64_t)zc * plane + (int64_t)gy * W) / 16 + gq));
+#pragma unroll
+    for (int k = 0; k < PERM; ++k) {
+      const int i = tid + k * MT;
+      if (i < NS) {
+        const int r = i / G::IX, q = i - r * G::IX;
+        const int gy = clampi(y0 - hy + r, H - 1), gq = clampi(xc0 - hx + q, nxc - 1);
+        pf[k] = __ldg(src4 + ((int64_t)zc * plane + (int64_t)gy * W) / 16 + gq);
+      }
     }
   };
+  auto load_plane = [&](int zv, int slot) {
+#pragma unroll
+    for (int k = 0; k < PERM; ++k) {
+      const int i = tid + k * MT;
+      if (i < NS) in[slot][i] = nzmask(pf[k]);
+    }
+    if (zv + 1 <= last_in) fetch(zv + 1);
+  };
+  fetch(z0 - ITER);
   auto store = [&](int zo, int r, int q, uint4 m) {
     const int gy = y0 + r, gq = xc0 + q;
     if (gy < H && gq < nxc) {

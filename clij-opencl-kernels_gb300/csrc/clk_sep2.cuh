@@ -34,7 +34,7 @@ struct Params {
   float wx[16];        // Gaussian: folded, normalised taps of X (w[0] centre, w[k] for +-k)
   float wy[16];        //           ... of Y
   float wz[kMaxCz + 1];  //         ... of Z
-  uint64_t mx, mz;     // mean: reciprocal multipliers for N = 2R+1 and 2cz+1
+  uint32_t mx, mz;     // mean: reciprocal multipliers (recip32) for N = 2R+1 and 2cz+1
   int cz;
 };
 
@@ -81,12 +81,22 @@ __device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
 }
 __device__ __forceinline__ uint64_t f2_bcast(float w) { return f2_pack(w, w); }
 
-// exact truncating division of an integer sum by N (see header comment)
-__device__ __forceinline__ int div_exact(int s, uint64_t m) {
-  const uint32_t a = (uint32_t)(s < 0 ? -s : s);
-  const int q = (int)(((uint64_t)a * m) >> 40);
-  return s < 0 ? -q : q;
+// Exact truncating division of an integer sum by N: m = ceil(2^32 / N) for
+// N >= 2 (m = 0 for N = 1).  For |s| < 2^24 and N < 256,
+// floor(|s| * m / 2^32) = floor(|s| / N): the error |s|(m - 2^32/N)/2^32 <
+// 2^-8 stays below the 1/N gap to the next quotient.  That quotient also
+// equals trunc(fl(s / N)) in float: s/N = q + r/N lies at least 1/N below
+// q + 1, more than half a float ulp at that magnitude (q < 2^24 / N).
+template <bool SIGNED> __device__ __forceinline__ int div_exact(int s, uint32_t m) {
+  if constexpr (SIGNED) {
+    const uint32_t a = (uint32_t)(s < 0 ? -s : s);
+    const int q = m ? (int)__umulhi(a, m) : (int)a;
+    return s < 0 ? -q : q;
+  } else {
+    return m ? (int)__umulhi((uint32_t)s, m) : s;
+  }
 }
+inline uint32_t recip32(int n) { return n <= 1 ? 0u : (uint32_t)((((uint64_t)1 << 32) + (uint64_t)n - 1) / (uint64_t)n); }
 
 template <class T> struct Is16;  // 16-bit lane traits of 8/16-bit pixels
 template <> struct Is16<uint16_t> { static constexpr bool sgn = false; };

@@ -37,18 +37,41 @@ template <class S> __device__ __forceinline__ float tofloat(S v) {
   }
 }
 
-// Geometry of one tile.  With TMA the staged row starts RA >= R elements left
-// of the tile (RA rounds R up so that the box's x coordinate is 16-byte
-// aligned) and the halo tile is double-buffered.
-template <class S, int OP, int R, bool TMA = false> struct Geo {
+// How the halo tile reaches shared memory.
+enum Stage {
+  STAGE_SCALAR = 0,  // one clamped pixel load per element (any layout)
+  STAGE_VEC = 1,     // 8/16-byte vector loads (rows and image base aligned)
+  STAGE_TMA = 2      // cp.async.bulk.tensor boxes, double-buffered
+};
+
+// Geometry of one tile.  The vector and TMA stagings start the staged row
+// RA >= R elements left of the tile, RA rounded up so that every staged
+// vector (TMA: the box origin) is aligned; the X pass then reads from column
+// RA - R.
+template <class S, int OP, int R, int MODE = STAGE_SCALAR> struct Geo {
   typedef typename Temp<S, OP>::T T;
-  static constexpr int RA = TMA ? (R + (16 / (int)sizeof(S)) - 1) / (16 / (int)sizeof(S)) * (16 / (int)sizeof(S)) : R;
+  static constexpr int ES = (int)sizeof(S);
+  static constexpr int rnd(int v, int m) { return (v + m - 1) / m * m; }
+  // staging vector bytes: 16 unless 8-byte vectors need a narrower margin
+  static constexpr int SV = MODE == STAGE_TMA ? 16
+                            : MODE == STAGE_VEC ? (rnd(R, 16 / ES) == rnd(R, 8 / ES) ? 16 : 8)
+                                                : ES;
+  static constexpr int RA = MODE == STAGE_SCALAR ? R : rnd(R, SV / ES);
   static constexpr int RW = TX + 2 * RA, RH = TY + 2 * R;
   static constexpr int NEL = RW * RH;
   static constexpr int PER = (NEL + NT - 1) / NT;
-  static constexpr int NBUF = TMA ? 2 : 1;
+  static constexpr int VE = SV / ES;          // pixels per staging vector
+  static constexpr int SR = RW / VE;          // staging vectors per row
+  static constexpr int NSLOT = RH * SR;
+  static constexpr int PERV = (NSLOT + NT - 1) / NT;
+  static constexpr int NBUF = MODE == STAGE_TMA ? 2 : 1;
   static constexpr int WIN_X = SEGX + 2 * R;
   static constexpr int WIN_Y = SEGY + 2 * R;
+  static constexpr int XOFF = RA - R;         // first staged column the X pass reads
+  // X pass of the aligned stagings: 16- (8-bit pixels: 8-) byte smem reads
+  // of the words covering columns [XOFF, XOFF + WIN_X) of a segment
+  static constexpr int XV = (SEGX * ES) % 16 == 0 ? 16 : 8;
+  static constexpr int NWD = rnd((XOFF + WIN_X) * ES, XV) / 4;
   static constexpr size_t buf_bytes() { return ((size_t)NEL * sizeof(S) + 127) & ~size_t(127); }
   static constexpr size_t tin_bytes() { return NBUF * buf_bytes(); }
   static constexpr size_t xs_bytes() { return ((size_t)RH * TX * sizeof(T) + 15) & ~size_t(15); }
@@ -56,18 +79,114 @@ template <class S, int OP, int R, bool TMA = false> struct Geo {
   static size_t smem(int cz) { return tin_bytes() + xs_bytes() + ring_bytes(cz); }
 };
 
+// ---------------------------------------------------------------- words
+// Element e of a staged row held in 32-bit words w (x fastest), for the
+// aligned stagings.  e is a compile-time constant after unrolling, so each
+// is a byte permute or a shift pair (plus an AND / XOR / float add).
+template <class S, int N> __device__ __forceinline__ uint32_t lanes16_of(const uint32_t (&w0)[N],
+                                                                       const uint32_t (&w1)[N], int e) {
+  // 16-bit lanes (row 0 low, row 1 high), as lane16 would widen them
+  if constexpr (sizeof(S) == 2) {
+    return __byte_perm(w0[e >> 1], w1[e >> 1], (e & 1) ? 0x7632 : 0x5410);
+  } else {
+    const uint32_t b = e & 3;
+    if constexpr (Is16<S>::sgn) {  // sign-extended bytes (shifts: __byte_perm has no sign mode)
+      const uint32_t lo = (uint32_t)((int)(w0[e >> 2] << (24 - 8 * b)) >> 24) & 0xFFFFu;
+      const uint32_t hi = (uint32_t)((int)(w1[e >> 2] << (24 - 8 * b)) >> 24) << 16;
+      return lo | hi;
+    } else {
+      return __byte_perm(w0[e >> 2], w1[e >> 2], b | ((4 + b) << 8)) & 0x00FF00FFu;
+    }
+  }
+}
+template <class S, int N> __device__ __forceinline__ int int_of(const uint32_t (&w)[N], int e) {
+  if constexpr (sizeof(S) == 2) {
+    if constexpr (Is16<S>::sgn) return (e & 1) ? (int)w[e >> 1] >> 16 : (int)(w[e >> 1] << 16) >> 16;
+    else return (int)((e & 1) ? w[e >> 1] >> 16 : w[e >> 1] & 0xFFFFu);
+  } else {
+    const uint32_t b = e & 3;
+    if constexpr (Is16<S>::sgn) return (int)(w[e >> 2] << (24 - 8 * b)) >> 24;
+    else return (int)__byte_perm(w[e >> 2], 0, b | 0x4440u);
+  }
+}
+// (row 0, row 1) values of element e as an f32x2 pair: float pixels as they
+// are; 8/16-bit pixels as the float 2^23 + v (+ bias for signed) built by a
+// byte permute, minus the same constant (exact)
+template <class S, int N> __device__ __forceinline__ uint64_t f2_of(const uint32_t (&w0)[N], const uint32_t (&w1)[N],
+                                                                  int e) {
+  if constexpr (sizeof(S) == 4) {
+    return f2_pack(__uint_as_float(w0[e]), __uint_as_float(w1[e]));
+  } else {
+    constexpr uint32_t K = 0x4B000000u;  // bytes 4..7 of the permute: 00 00 00 4B
+    uint32_t a, b;
+    if constexpr (sizeof(S) == 2) {
+      const uint32_t h = 2 * (e & 1), sel = h | ((h + 1) << 4) | 0x7400u;
+      a = __byte_perm(w0[e >> 1], K, sel);
+      b = __byte_perm(w1[e >> 1], K, sel);
+    } else {
+      const uint32_t sel = (e & 3) | 0x7440u;
+      a = __byte_perm(w0[e >> 2], K, sel);
+      b = __byte_perm(w1[e >> 2], K, sel);
+    }
+    constexpr uint32_t flip = Is16<S>::sgn ? (sizeof(S) == 2 ? 0x8000u : 0x80u) : 0u;
+    constexpr float off = 8388608.0f + (Is16<S>::sgn ? (sizeof(S) == 2 ? 32768.0f : 128.0f) : 0.0f);
+    if constexpr (flip != 0) a ^= flip, b ^= flip;
+    return f2_add(f2_pack(__uint_as_float(a), __uint_as_float(b)), f2_bcast(-off));
+  }
+}
+
+// a 32-bit word of a pixel value repeated (clamp-to-edge fill of a vector)
+template <class S> __device__ __forceinline__ uint32_t splat_word(S v) {
+  if constexpr (sizeof(S) == 4) return __float_as_uint(v);
+  else if constexpr (sizeof(S) == 2) return (uint32_t)(uint16_t)v * 0x10001u;
+  else return (uint32_t)(uint8_t)v * 0x01010101u;
+}
+
+// Running min/max of M consecutive windows of 2R+1 packed lanes:
+// out[j] = op(win[j .. j+2R]).  When every window contains the split point
+// M (2R >= M), out[j] = op(suffix of win[j .. M-1], prefix of win[M .. j+2R])
+// (the van Herk / Gil-Werman decomposition): 2R + 2M - 2 operations instead
+// of 2R * M.  Exact for min/max, so the result is the same either way.
+template <class S, int OP, int M, int R>
+__device__ __forceinline__ void window_minmax(const uint32_t (&win)[M + 2 * R], uint32_t (&out)[M]) {
+  if constexpr (2 * R >= M && M > 1) {
+    uint32_t suf[M];
+    suf[M - 1] = win[M - 1];
+#pragma unroll
+    for (int j = M - 2; j >= 0; --j) suf[j] = mm<S, OP>(win[j], suf[j + 1]);
+    uint32_t pre = win[M];
+#pragma unroll
+    for (int k = M + 1; k <= 2 * R; ++k) pre = mm<S, OP>(pre, win[k]);
+    out[0] = mm<S, OP>(suf[0], pre);  // window 0 ends at 2R
+#pragma unroll
+    for (int j = 1; j < M; ++j) {
+      pre = mm<S, OP>(pre, win[j + 2 * R]);
+      out[j] = mm<S, OP>(suf[j], pre);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+      uint32_t a = win[j];
+#pragma unroll
+      for (int k = 1; k <= 2 * R; ++k) a = mm<S, OP>(a, win[j + k]);
+      out[j] = a;
+    }
+  }
+}
+
 // One tile (bx, by) x z-chunk bz of one image; the whole CTA takes part.
 // smem: dynamic shared memory of at least Geo::smem(p.cz) bytes (128-byte
 // aligned).  TMA: map is a 3-D tensor map of src with a (RW, RH, 1) box;
 // err receives 1 if a bounded wait for a tile ran out (the tile is then
 // abandoned).
-template <class S, class D, int OP, int R, bool TMA = false>
+template <class S, class D, int OP, int R, int MODE = STAGE_SCALAR>
 __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restrict__ dst, int W, int H, int Dz,
                                           int zchunk, const Params& p, int bx, int by, int bz,
                                           unsigned char* smem, const CUtensorMap* map = nullptr,
                                           int* err = nullptr) {
-  using G = Geo<S, OP, R, TMA>;
+  using G = Geo<S, OP, R, MODE>;
   using T = typename G::T;
+  constexpr bool TMA = MODE == STAGE_TMA;
   S* tin = reinterpret_cast<S*>(smem);
   T* xs = reinterpret_cast<T*>(smem + G::tin_bytes());
   T* ring = reinterpret_cast<T*>(smem + G::tin_bytes() + G::xs_bytes());
@@ -76,25 +195,58 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
   const int x0 = bx * TX, y0 = by * TY;
   const int z0 = bz * zchunk, z1 = min(Dz, z0 + zchunk);
   const int64_t plane = (int64_t)W * H;
-  constexpr int XOFF = G::RA - R;  // first staged column the X pass reads
+  constexpr int XOFF = G::XOFF;
 
-  S pre[G::PER];  // unused (and removed) when TMA stages the tile
+  // register prefetch of the next plane's halo tile (scalar / vector staging)
+  typedef typename std::conditional<G::SV == 16, uint4, uint2>::type VT;
+  S pre[MODE == STAGE_SCALAR ? G::PER : 1];
+  VT prev[MODE == STAGE_VEC ? G::PERV : 1];
   auto fetch = [&](int zv) {
     const S* sp = src + (int64_t)clampi(zv, Dz - 1) * plane;
+    if constexpr (MODE == STAGE_SCALAR) {
 #pragma unroll
-    for (int k = 0; k < G::PER; ++k) {
-      const int i = tid + k * NT;
-      if (i < G::NEL) {
-        const int r = i / G::RW, q = i - r * G::RW;
-        pre[k] = __ldg(sp + (int64_t)clampi(y0 - R + r, H - 1) * W + clampi(x0 - R + q, W - 1));
+      for (int k = 0; k < G::PER; ++k) {
+        const int i = tid + k * NT;
+        if (i < G::NEL) {
+          const int r = i / G::RW, q = i - r * G::RW;
+          pre[k] = __ldg(sp + (int64_t)clampi(y0 - R + r, H - 1) * W + clampi(x0 - R + q, W - 1));
+        }
+      }
+    } else if constexpr (MODE == STAGE_VEC) {
+      // a vector lies wholly inside the row or wholly outside it (rows and
+      // the staged origin are vector-aligned): load it, or fill it with the
+      // clamped edge pixel
+#pragma unroll
+      for (int k = 0; k < G::PERV; ++k) {
+        const int sl = tid + k * NT;
+        if (k < G::PERV - 1 || sl < G::NSLOT) {
+          const int r = sl / G::SR, v = sl - r * G::SR;
+          const S* rowp = sp + (int64_t)clampi(y0 - R + r, H - 1) * W;
+          const int gx = x0 - G::RA + v * G::VE;
+          if (gx >= 0 && gx < W) {
+            prev[k] = __ldg(reinterpret_cast<const VT*>(rowp + gx));
+          } else {
+            const uint32_t w = splat_word<S>(__ldg(rowp + (gx < 0 ? 0 : W - 1)));
+            if constexpr (G::SV == 16) prev[k] = make_uint4(w, w, w, w);
+            else prev[k] = make_uint2(w, w);
+          }
+        }
       }
     }
   };
   auto commit = [&]() {
+    if constexpr (MODE == STAGE_SCALAR) {
 #pragma unroll
-    for (int k = 0; k < G::PER; ++k) {
-      const int i = tid + k * NT;
-      if (i < G::NEL) tin[i] = pre[k];
+      for (int k = 0; k < G::PER; ++k) {
+        const int i = tid + k * NT;
+        if (i < G::NEL) tin[i] = pre[k];
+      }
+    } else if constexpr (MODE == STAGE_VEC) {
+#pragma unroll
+      for (int k = 0; k < G::PERV; ++k) {
+        const int sl = tid + k * NT;
+        if (k < G::PERV - 1 || sl < G::NSLOT) reinterpret_cast<VT*>(tin)[sl] = prev[k];
+      }
     }
   };
 
@@ -140,6 +292,9 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
   // Y/Z ownership: column pair cp, rows sy*SEGY .. +SEGY-1
   const int cp = tid % (TX / 2), sy = tid / (TX / 2);
   int wslot = 0;
+  int zs0[SEGY], zs1[SEGY];  // mean: running sums along z of this thread's cells
+#pragma unroll
+  for (int j = 0; j < SEGY; ++j) zs0[j] = zs1[j] = 0;
   for (int zi = z0 - cz, it = 0; zi < z1 + cz; ++zi, ++it) {
     S* tcur = tin;
     if constexpr (TMA) {
@@ -158,7 +313,7 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
         fix_border(tcur);
         __syncthreads();
       }
-    } else {
+    } else {  // scalar / vector staging from the register prefetch
       __syncthreads();  // previous X pass done with tin, previous Y pass with xs
       commit();
       if (zi + 1 < z1 + cz) fetch(zi + 1);
@@ -173,37 +328,61 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
         const S* r1 = r0 + G::RW;
         T* o0 = xs + (2 * rp) * TX + sg * SEGX;
         T* o1 = o0 + TX;
+        // aligned stagings: the segment's words of both rows, read as vectors
+        uint32_t w0[MODE == STAGE_SCALAR ? 1 : G::NWD], w1[MODE == STAGE_SCALAR ? 1 : G::NWD];
+        if constexpr (MODE != STAGE_SCALAR) {
+          const S* a0 = tcur + (2 * rp) * G::RW + sg * SEGX;
+          if constexpr (G::XV == 16) {
+#pragma unroll
+            for (int v = 0; v < G::NWD / 4; ++v) {
+              const uint4 x = reinterpret_cast<const uint4*>(a0)[v];
+              const uint4 y = reinterpret_cast<const uint4*>(a0 + G::RW)[v];
+              w0[4 * v] = x.x, w0[4 * v + 1] = x.y, w0[4 * v + 2] = x.z, w0[4 * v + 3] = x.w;
+              w1[4 * v] = y.x, w1[4 * v + 1] = y.y, w1[4 * v + 2] = y.z, w1[4 * v + 3] = y.w;
+            }
+          } else {
+#pragma unroll
+            for (int v = 0; v < G::NWD / 2; ++v) {
+              const uint2 x = reinterpret_cast<const uint2*>(a0)[v];
+              const uint2 y = reinterpret_cast<const uint2*>(a0 + G::RW)[v];
+              w0[2 * v] = x.x, w0[2 * v + 1] = x.y;
+              w1[2 * v] = y.x, w1[2 * v + 1] = y.y;
+            }
+          }
+        }
         if constexpr (OP == MIN || OP == MAX) {
           uint32_t win[G::WIN_X];
 #pragma unroll
-          for (int k = 0; k < G::WIN_X; ++k) win[k] = lane16(r0[k]) | (lane16(r1[k]) << 16);
+          for (int k = 0; k < G::WIN_X; ++k) {
+            if constexpr (MODE == STAGE_SCALAR) win[k] = lane16(r0[k]) | (lane16(r1[k]) << 16);
+            else win[k] = lanes16_of<S>(w0, w1, XOFF + k);
+          }
+          uint32_t out[SEGX];
+          window_minmax<S, OP, SEGX, R>(win, out);
 #pragma unroll
           for (int j = 0; j < SEGX; j += 2) {
-            uint32_t a = win[j], b = win[j + 1];
-#pragma unroll
-            for (int k = 1; k <= 2 * R; ++k) {
-              a = mm<S, OP>(a, win[j + k]);
-              b = mm<S, OP>(b, win[j + 1 + k]);
-            }
-            *reinterpret_cast<uint32_t*>(o0 + j) = __byte_perm(a, b, 0x5410);
-            *reinterpret_cast<uint32_t*>(o1 + j) = __byte_perm(a, b, 0x7632);
+            *reinterpret_cast<uint32_t*>(o0 + j) = __byte_perm(out[j], out[j + 1], 0x5410);
+            *reinterpret_cast<uint32_t*>(o1 + j) = __byte_perm(out[j], out[j + 1], 0x7632);
           }
         } else if constexpr (OP == MEAN) {
-          int w0[G::WIN_X], w1[G::WIN_X];
+          int v0[G::WIN_X], v1[G::WIN_X];
 #pragma unroll
-          for (int k = 0; k < G::WIN_X; ++k) w0[k] = (int)r0[k], w1[k] = (int)r1[k];
+          for (int k = 0; k < G::WIN_X; ++k) {
+            if constexpr (MODE == STAGE_SCALAR) v0[k] = (int)r0[k], v1[k] = (int)r1[k];
+            else v0[k] = int_of<S>(w0, XOFF + k), v1[k] = int_of<S>(w1, XOFF + k);
+          }
           int s0 = 0, s1 = 0;
 #pragma unroll
-          for (int k = 0; k <= 2 * R; ++k) s0 += w0[k], s1 += w1[k];
+          for (int k = 0; k <= 2 * R; ++k) s0 += v0[k], s1 += v1[k];
           int q0[SEGX], q1[SEGX];
 #pragma unroll
           for (int j = 0; j < SEGX; ++j) {
             if (j > 0) {
-              s0 += w0[j + 2 * R] - w0[j - 1];
-              s1 += w1[j + 2 * R] - w1[j - 1];
+              s0 += v0[j + 2 * R] - v0[j - 1];
+              s1 += v1[j + 2 * R] - v1[j - 1];
             }
-            q0[j] = div_exact(s0, p.mx);
-            q1[j] = div_exact(s1, p.mx);
+            q0[j] = div_exact<Is16<S>::sgn>(s0, p.mx);
+            q1[j] = div_exact<Is16<S>::sgn>(s1, p.mx);
           }
 #pragma unroll
           for (int j = 0; j < SEGX; j += 2) {
@@ -213,7 +392,10 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
         } else {
           uint64_t win[G::WIN_X];
 #pragma unroll
-          for (int k = 0; k < G::WIN_X; ++k) win[k] = f2_pack(tofloat(r0[k]), tofloat(r1[k]));
+          for (int k = 0; k < G::WIN_X; ++k) {
+            if constexpr (MODE == STAGE_SCALAR) win[k] = f2_pack(tofloat(r0[k]), tofloat(r1[k]));
+            else win[k] = f2_of<S>(w0, w1, XOFF + k);
+          }
           uint64_t out[SEGX];
 #pragma unroll
           for (int j = 0; j < SEGX; ++j) {
@@ -231,7 +413,9 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
         }
       }
     }
-    if constexpr (TMA) tma::fence_proxy_async();  // this thread's reads/writes of tcur before the refill
+    if constexpr (TMA) {
+      if (border) tma::fence_proxy_async();  // this thread's fix-up writes of tcur before the refill
+    }
     __syncthreads();
     if constexpr (TMA) {
       if (tid == 0 && zi + 2 < z1 + cz) issue(zi + 2, it & 1);
@@ -246,13 +430,10 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
         uint32_t win[G::WIN_Y];
 #pragma unroll
         for (int k = 0; k < G::WIN_Y; ++k) win[k] = *reinterpret_cast<const uint32_t*>(col + k * TX);
+        uint32_t out[SEGY];
+        window_minmax<S, OP, SEGY, R>(win, out);
 #pragma unroll
-        for (int j = 0; j < SEGY; ++j) {
-          uint32_t a = win[j];
-#pragma unroll
-          for (int k = 1; k <= 2 * R; ++k) a = mm<S, OP>(a, win[j + k]);
-          *reinterpret_cast<uint32_t*>(o + j * TX) = a;
-        }
+        for (int j = 0; j < SEGY; ++j) *reinterpret_cast<uint32_t*>(o + j * TX) = out[j];
       } else if constexpr (OP == MEAN) {
         int w0[G::WIN_Y], w1[G::WIN_Y];
 #pragma unroll
@@ -266,8 +447,10 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
             s0 += w0[j + 2 * R] - w0[j - 1];
             s1 += w1[j + 2 * R] - w1[j - 1];
           }
-          *reinterpret_cast<uint32_t*>(o + j * TX) =
-              __byte_perm((uint32_t)div_exact(s0, p.mx), (uint32_t)div_exact(s1, p.mx), 0x5410);
+          const int q0 = div_exact<Is16<S>::sgn>(s0, p.mx), q1 = div_exact<Is16<S>::sgn>(s1, p.mx);
+          *reinterpret_cast<uint32_t*>(o + j * TX) = __byte_perm((uint32_t)q0, (uint32_t)q1, 0x5410);
+          zs0[j] += q0;  // the new plane enters the running z sums
+          zs1[j] += q1;
         }
       } else {
         uint64_t win[G::WIN_Y];
@@ -284,67 +467,93 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
     }
 
     // ---------------- Z pass over this thread's own ring cells
+    // (ring slots in the outer loop, the thread's SEGY rows in the inner one)
     const int zo = zi - cz;
     const int oldest = wslot + 1 == NZ ? 0 : wslot + 1;
     wslot = oldest;
     if (zo >= z0) {
+      constexpr int PL = TY * TX;  // one ring plane, in T elements
+      const T* cells = ring + (sy * SEGY) * TX + 2 * cp;
       const int gx = x0 + 2 * cp;
+      // even widths keep every row pair-aligned: one store for both lanes;
+      // odd widths store the lanes separately (the second may lie past W)
+      const bool pair = (W & 1) == 0;
+      if constexpr (OP == MIN || OP == MAX) {
+        uint32_t a[SEGY];
+        const T* c = cells + (size_t)oldest * PL;
 #pragma unroll
-      for (int j = 0; j < SEGY; ++j) {
-        const int gy = y0 + sy * SEGY + j;
-        const size_t cell = (size_t)(sy * SEGY + j) * TX + 2 * cp;
-        D* out = dst + (int64_t)zo * plane + (int64_t)gy * W + gx;
-        const bool ok = gy < H && gx < W;
-        // even widths keep every row pair-aligned: one store for both lanes;
-        // odd widths store the lanes separately (the second may lie past W)
-        const bool pair = (W & 1) == 0;
-        if constexpr (OP == MIN || OP == MAX) {
-          uint32_t a = *reinterpret_cast<const uint32_t*>(ring + (size_t)oldest * TY * TX + cell);
-          int idx = oldest;
-          for (int v = 1; v < NZ; ++v) {
-            idx = idx + 1 == NZ ? 0 : idx + 1;
-            a = mm<S, OP>(a, *reinterpret_cast<const uint32_t*>(ring + (size_t)idx * TY * TX + cell));
+        for (int j = 0; j < SEGY; ++j) a[j] = *reinterpret_cast<const uint32_t*>(c + j * TX);
+        int idx = oldest;
+        for (int v = 1; v < NZ; ++v) {
+          idx = idx + 1 == NZ ? 0 : idx + 1;
+          c = cells + (size_t)idx * PL;
+#pragma unroll
+          for (int j = 0; j < SEGY; ++j) a[j] = mm<S, OP>(a[j], *reinterpret_cast<const uint32_t*>(c + j * TX));
+        }
+#pragma unroll
+        for (int j = 0; j < SEGY; ++j) {
+          const int gy = y0 + sy * SEGY + j;
+          D* out = dst + (int64_t)zo * plane + (int64_t)gy * W + gx;
+          if (gy < H && gx < W) {
+            if (pair) {
+              if constexpr (sizeof(D) == 2) *reinterpret_cast<uint32_t*>(out) = a[j];
+              else *reinterpret_cast<uint16_t*>(out) = (uint16_t)__byte_perm(a[j], 0, 0x0020);
+            } else {
+              out[0] = from_lane16<D>(a[j] & 0xFFFFu);
+              if (gx + 1 < W) out[1] = from_lane16<D>(a[j] >> 16);
+            }
           }
-          if (ok && pair) {
-            if constexpr (sizeof(D) == 2) *reinterpret_cast<uint32_t*>(out) = a;
-            else *reinterpret_cast<uint16_t*>(out) = (uint16_t)__byte_perm(a, 0, 0x0020);
-          } else if (ok) {
-            out[0] = from_lane16<D>(a & 0xFFFFu);
-            if (gx + 1 < W) out[1] = from_lane16<D>(a >> 16);
+        }
+      } else if constexpr (OP == MEAN) {
+        // zs holds the NZ planes zo-cz .. zo+cz; the oldest (zo-cz) leaves
+        const T* c = cells + (size_t)oldest * PL;
+#pragma unroll
+        for (int j = 0; j < SEGY; ++j) {
+          const int q0 = div_exact<Is16<S>::sgn>(zs0[j], p.mz), q1 = div_exact<Is16<S>::sgn>(zs1[j], p.mz);
+          zs0[j] -= (int)c[j * TX];
+          zs1[j] -= (int)c[j * TX + 1];
+          const int gy = y0 + sy * SEGY + j;
+          D* out = dst + (int64_t)zo * plane + (int64_t)gy * W + gx;
+          if (gy < H && gx < W) {
+            if (pair) {
+              if constexpr (sizeof(D) == 2) *reinterpret_cast<uint32_t*>(out) = __byte_perm(q0, q1, 0x5410);
+              else *reinterpret_cast<uint16_t*>(out) = (uint16_t)__byte_perm(q0, q1, 0x0040);
+            } else {
+              out[0] = (D)q0;
+              if (gx + 1 < W) out[1] = (D)q1;
+            }
           }
-        } else if constexpr (OP == MEAN) {
-          int s0 = 0, s1 = 0, idx = oldest;
-          for (int v = 0; v < NZ; ++v) {
-            const T* c = ring + (size_t)idx * TY * TX + cell;
-            s0 += (int)c[0];
-            s1 += (int)c[1];
-            idx = idx + 1 == NZ ? 0 : idx + 1;
-          }
-          const int q0 = div_exact(s0, p.mz), q1 = div_exact(s1, p.mz);
-          if (ok && pair) {
-            if constexpr (sizeof(D) == 2) *reinterpret_cast<uint32_t*>(out) = __byte_perm(q0, q1, 0x5410);
-            else *reinterpret_cast<uint16_t*>(out) = (uint16_t)__byte_perm(q0, q1, 0x0040);
-          } else if (ok) {
-            out[0] = (D)q0;
-            if (gx + 1 < W) out[1] = (D)q1;
-          }
-        } else {
-          const int centre = oldest + cz >= NZ ? oldest + cz - NZ : oldest + cz;
-          const uint64_t* base = reinterpret_cast<const uint64_t*>(ring + cell);
-          const size_t stride = (size_t)TY * TX / 2;  // ring plane in uint64 units
-          uint64_t acc = f2_fma(f2_bcast(p.wz[0]), base[centre * stride], 0ull);
-          int lo = centre, hi = centre;
-          for (int k = 1; k <= cz; ++k) {
-            lo = lo == 0 ? NZ - 1 : lo - 1;
-            hi = hi + 1 == NZ ? 0 : hi + 1;
-            acc = f2_fma(f2_bcast(p.wz[k]), f2_add(base[lo * stride], base[hi * stride]), acc);
-          }
-          if (ok && pair) {
-            *reinterpret_cast<uint64_t*>(out) = acc;
-          } else if (ok) {
-            const float2 f = f2_unpack(acc);
-            out[0] = f.x;
-            if (gx + 1 < W) out[1] = f.y;
+        }
+      } else {
+        const int centre = oldest + cz >= NZ ? oldest + cz - NZ : oldest + cz;
+        const uint64_t* base = reinterpret_cast<const uint64_t*>(cells);
+        constexpr int stride = PL / 2;  // ring plane in uint64 units
+        constexpr int rstride = TX / 2;  // row in uint64 units
+        uint64_t acc[SEGY];
+#pragma unroll
+        for (int j = 0; j < SEGY; ++j) acc[j] = f2_fma(f2_bcast(p.wz[0]), base[centre * stride + j * rstride], 0ull);
+        int lo = centre, hi = centre;
+        for (int k = 1; k <= cz; ++k) {
+          lo = lo == 0 ? NZ - 1 : lo - 1;
+          hi = hi + 1 == NZ ? 0 : hi + 1;
+          const uint64_t* bl = base + lo * stride;
+          const uint64_t* bh = base + hi * stride;
+          const uint64_t wk = f2_bcast(p.wz[k]);
+#pragma unroll
+          for (int j = 0; j < SEGY; ++j) acc[j] = f2_fma(wk, f2_add(bl[j * rstride], bh[j * rstride]), acc[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < SEGY; ++j) {
+          const int gy = y0 + sy * SEGY + j;
+          D* out = dst + (int64_t)zo * plane + (int64_t)gy * W + gx;
+          if (gy < H && gx < W) {
+            if (pair) {
+              *reinterpret_cast<uint64_t*>(out) = acc[j];
+            } else {
+              const float2 f = f2_unpack(acc[j]);
+              out[0] = f.x;
+              if (gx + 1 < W) out[1] = f.y;
+            }
           }
         }
       }
@@ -352,11 +561,15 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
   }
 }
 
-template <class S, class D, int OP, int R>
-__global__ void __launch_bounds__(NT) k_sep2(const S* __restrict__ src, D* __restrict__ dst, int W, int H, int Dz,
-                                             int zchunk, const __grid_constant__ Params p) {
+// CTAs per SM the register budget is sized for (85 / 128 registers)
+template <int OP> constexpr int min_ctas() { return OP == GAUSS ? 2 : 3; }
+
+template <class S, class D, int OP, int R, int MODE>
+__global__ void __launch_bounds__(NT, min_ctas<OP>()) k_sep2(const S* __restrict__ src, D* __restrict__ dst, int W,
+                                                             int H, int Dz, int zchunk,
+                                                             const __grid_constant__ Params p) {
   extern __shared__ __align__(128) unsigned char smem[];
-  sep2_tile<S, D, OP, R>(src, dst, W, H, Dz, zchunk, p, blockIdx.x, blockIdx.y, blockIdx.z, smem);
+  sep2_tile<S, D, OP, R, MODE>(src, dst, W, H, Dz, zchunk, p, blockIdx.x, blockIdx.y, blockIdx.z, smem);
 }
 
 // Same tile body with the halo tile staged by TMA, double-buffered: the copy
@@ -366,8 +579,8 @@ __global__ void __launch_bounds__(NT) k_sep2_tma(const __grid_constant__ CUtenso
                                                  int W, int H, int Dz, int zchunk, const __grid_constant__ Params p,
                                                  int* err) {
   extern __shared__ __align__(128) unsigned char smem[];
-  sep2_tile<S, D, OP, R, true>(nullptr, dst, W, H, Dz, zchunk, p, blockIdx.x, blockIdx.y, blockIdx.z, smem, &map,
-                               err);
+  sep2_tile<S, D, OP, R, STAGE_TMA>(nullptr, dst, W, H, Dz, zchunk, p, blockIdx.x, blockIdx.y, blockIdx.z, smem,
+                                    &map, err);
 }
 
 template <class K>
@@ -381,11 +594,12 @@ bool smem_ok(K kern, size_t smem) {
   return true;
 }
 
-// CLK_SEP2_TMA=0 in the environment keeps the register-prefetch staging
+// CLK_SEP2_TMA=1 in the environment stages with TMA instead of the
+// register prefetch
 inline bool tma_enabled() {
   static const bool on = [] {
     const char* e = getenv("CLK_SEP2_TMA");
-    return !(e && e[0] == '0');
+    return e && e[0] == '1';
   }();
   return on;
 }
@@ -401,7 +615,7 @@ clk_status launch(const Image& dst, const Image& src, const Params& p, cudaStrea
   const int zchunk = (dst.d + chunks - 1) / chunks;
   const dim3 grid(tx, ty, (dst.d + zchunk - 1) / zchunk);
 
-  using GT = Geo<S, OP, R, true>;
+  using GT = Geo<S, OP, R, STAGE_TMA>;
   CUtensorMap map;
   int* err = wait_flag_device();
   if (tma_enabled() && err && smem_ok(k_sep2_tma<S, D, OP, R>, GT::smem(p.cz)) &&
@@ -410,10 +624,19 @@ clk_status launch(const Image& dst, const Image& src, const Params& p, cudaStrea
     count_launch();
     return check_launch("separable (fused, sep2, tma)");
   }
-  using G = Geo<S, OP, R>;
-  if (!smem_ok(k_sep2<S, D, OP, R>, G::smem(p.cz))) return CLK_UNSUPPORTED_DTYPE;
-  k_sep2<S, D, OP, R><<<grid, NT, G::smem(p.cz), st>>>((const S*)src.ptr, (D*)dst.ptr, dst.w, dst.h, dst.d, zchunk,
-                                                       p);
+  // vector staging when the image base and rows are aligned to its vectors
+  using GV = Geo<S, OP, R, STAGE_VEC>;
+  if ((uintptr_t)src.ptr % GV::SV == 0 && ((int64_t)src.w * (int64_t)sizeof(S)) % GV::SV == 0 &&
+      smem_ok(k_sep2<S, D, OP, R, STAGE_VEC>, GV::smem(p.cz))) {
+    k_sep2<S, D, OP, R, STAGE_VEC><<<grid, NT, GV::smem(p.cz), st>>>((const S*)src.ptr, (D*)dst.ptr, dst.w, dst.h,
+                                                                     dst.d, zchunk, p);
+    count_launch();
+    return check_launch("separable (fused, sep2, vector staging)");
+  }
+  using G = Geo<S, OP, R, STAGE_SCALAR>;
+  if (!smem_ok(k_sep2<S, D, OP, R, STAGE_SCALAR>, G::smem(p.cz))) return CLK_UNSUPPORTED_DTYPE;
+  k_sep2<S, D, OP, R, STAGE_SCALAR><<<grid, NT, G::smem(p.cz), st>>>((const S*)src.ptr, (D*)dst.ptr, dst.w, dst.h,
+                                                                     dst.d, zchunk, p);
   count_launch();
   return check_launch("separable (fused, sep2)");
 }
@@ -430,7 +653,6 @@ clk_status by_radius(int R, const Image& dst, const Image& src, const Params& p,
 constexpr int kMaxRIntegers = 8;
 constexpr int kMaxRGauss = 12;
 
-uint64_t recip40(int n) { return (((uint64_t)1 << 40) + (uint64_t)n - 1) / (uint64_t)n; }
 
 bool layout_ok(const Image& dst, const Image& src, int align_elems) {
   return src.w == dst.w && src.h == dst.h && src.d == dst.d &&

@@ -10,8 +10,8 @@ clk_status sep2_mean(int R, const Image& dst, const Image& src, int cz, cudaStre
     return CLK_UNSUPPORTED_DTYPE;
   Params p{};
   p.cz = cz;
-  p.mx = recip40(2 * R + 1);
-  p.mz = recip40(2 * cz + 1);
+  p.mx = recip32(2 * R + 1);
+  p.mz = recip32(2 * cz + 1);
   switch (src.dt) {
     case CLK_U16: return by_radius<uint16_t, uint16_t, MEAN, kMaxRIntegers>(R, dst, src, p, st);
     case CLK_I16: return by_radius<int16_t, int16_t, MEAN, kMaxRIntegers>(R, dst, src, p, st);

@@ -20,7 +20,13 @@
 // outputs use the generic kernel, which sums in the reference's order.
 //
 // A thread owns 2 x 2 outputs (x, x+1; y, y+1) and walks along z, keeping
-// A, B, C of the last three planes in registers.
+// A, B, C of the last three planes in registers (the z loop is unrolled by
+// three so the ring never moves) and the next plane's pixels in flight.
+// Rows are read as aligned pixel pairs.  Sums convert to float exactly
+// without the I2F unit; the square root is the hardware approximation
+// (relative error far below the 1e-5 bound).
+#include <type_traits>
+
 #include "clk_common.cuh"
 
 namespace clk {
@@ -63,34 +69,95 @@ __device__ __noinline__ float3 wrap_counts(const S* __restrict__ src, int W, int
   return make_float3(kx, ky, kz);
 }
 
+// Two consecutive pixels (x, x+1), x even, as one aligned load.
+template <class S> struct Pair;
+template <> struct Pair<uint16_t> {
+  typedef uint32_t V;
+  static __device__ __forceinline__ int lo(V v) { return (int)(v & 0xFFFFu); }
+  static __device__ __forceinline__ int hi(V v) { return (int)(v >> 16); }
+};
+template <> struct Pair<int16_t> {
+  typedef uint32_t V;
+  static __device__ __forceinline__ int lo(V v) { return (int)(int16_t)(v & 0xFFFFu); }
+  static __device__ __forceinline__ int hi(V v) { return (int)v >> 16; }
+};
+template <> struct Pair<uint8_t> {
+  typedef uint16_t V;
+  static __device__ __forceinline__ int lo(V v) { return (int)(v & 0xFFu); }
+  static __device__ __forceinline__ int hi(V v) { return (int)(v >> 8); }
+};
+template <> struct Pair<int8_t> {
+  typedef uint16_t V;
+  static __device__ __forceinline__ int lo(V v) { return (int)(int8_t)(v & 0xFFu); }
+  static __device__ __forceinline__ int hi(V v) { return (int)(int8_t)(v >> 8); }
+};
+template <> struct Pair<float> {
+  typedef float2 V;
+  static __device__ __forceinline__ float lo(V v) { return v.x; }
+  static __device__ __forceinline__ float hi(V v) { return v.y; }
+};
+
+// int -> float without the I2F unit, exact for |v| < 2^22 (every sum here:
+// at most 47 * 65535 in magnitude)
+__device__ __forceinline__ float exact_float(int v) { return __int_as_float(0x4B400000 + v) - 12582912.0f; }
+__device__ __forceinline__ float exact_float(float v) { return v; }
+
+__device__ __forceinline__ float sqrt_approx(float v) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(v));
+  return r;
+}
+
 template <class S, bool WRAP>
-__global__ void __launch_bounds__(SBX * SBY) k_sobel3d_fast(const S* __restrict__ src, float* __restrict__ dst, int W,
-                                                            int H, int D, int zchunk) {
+__global__ void __launch_bounds__(SBX * SBY, 2) k_sobel3d_fast(const S* __restrict__ src, float* __restrict__ dst,
+                                                               int W, int H, int D, int zchunk) {
   using N = typename Num<S>::type;
+  using PV = typename Pair<S>::V;
   const int x = 2 * (blockIdx.x * SBX + threadIdx.x);
   const int y = 2 * (blockIdx.y * SBY + threadIdx.y);
   if (x >= W || y >= H) return;
   const int z0 = blockIdx.z * zchunk, z1 = min(D, z0 + zchunk);
   const int64_t plane = (int64_t)W * H;
+  const bool hasl = x > 0, hasr = x + 2 < W;
+  int roff[4];  // rows y-1 .. y+2, clamped
+#pragma unroll
+  for (int r = 0; r < 4; ++r) roff[r] = clampi(y - 1 + r, H - 1) * W + x;
 
-  // per output (ox, oy): A, B, C of planes p-3, p-2, p-1 (ring index 0..2)
+  // raw pairs (x-2, x-1), (x, x+1), (x+2, x+3) of the four rows of one plane
+  PV raw[4][3];
+  auto load = [&](int p) {
+    const S* sp = src + (int64_t)clampi(p, D - 1) * plane;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const PV* row = reinterpret_cast<const PV*>(sp + roff[r]);
+      raw[r][1] = __ldg(row);
+      raw[r][0] = hasl ? __ldg(row - 1) : raw[r][1];
+      raw[r][2] = hasr ? __ldg(row + 1) : raw[r][1];
+    }
+  };
+
+  // per output (ox, oy): A, B, C of the three planes before the newest
   N A[3][2][2], B[3][2][2], C[3][2][2];
+  N ex[2][2], ey[2][2], ez[2][2];
   uint32_t zflags = 0;  // bit i: a zero pixel among this thread's loads of plane p-i
 
-  // partial sums of plane p; also returns the E terms
-  auto plane_terms = [&](int p, N (&a)[2][2], N (&b)[2][2], N (&c)[2][2], N (&ex)[2][2], N (&ey)[2][2],
-                         N (&ez)[2][2]) {
-    const S* sp = src + (int64_t)clampi(p, D - 1) * plane;
-    N v[4][4];  // rows y-1 .. y+2, columns x-1 .. x+2
+  // partial sums of the plane held in raw, into ring slot s; E terms too
+  auto terms = [&](N (&a)[2][2], N (&b)[2][2], N (&c)[2][2]) {
+    N v[4][4];  // rows y-1 .. y+2, columns x-1 .. x+2 (clamped)
 #pragma unroll
-    for (int r = 0; r < 4; ++r) load4<S>(sp + (int64_t)clampi(y - 1 + r, H - 1) * W, x, W, v[r]);
+    for (int r = 0; r < 4; ++r) {
+      v[r][0] = hasl ? Pair<S>::hi(raw[r][0]) : Pair<S>::lo(raw[r][1]);
+      v[r][1] = Pair<S>::lo(raw[r][1]);
+      v[r][2] = Pair<S>::hi(raw[r][1]);
+      v[r][3] = hasr ? Pair<S>::lo(raw[r][2]) : Pair<S>::hi(raw[r][1]);
+    }
     if constexpr (WRAP) {
-      bool z = false;
+      N m = v[0][0];
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) z |= v[r][c] == 0;
-      zflags = (zflags << 1) | (z ? 1u : 0u);
+        for (int c = 0; c < 4; ++c) m = min(m, v[r][c]);
+      zflags = (zflags << 1) | (m == 0 ? 1u : 0u);
     }
     N sx[4][2], dx[4][2];
 #pragma unroll
@@ -115,22 +182,22 @@ __global__ void __launch_bounds__(SBX * SBY) k_sobel3d_fast(const S* __restrict_
       }
   };
 
-  N ex[2][2], ey[2][2], ez[2][2];
-  plane_terms(z0 - 1, A[0], B[0], C[0], ex, ey, ez);
-  plane_terms(z0, A[1], B[1], C[1], ex, ey, ez);
-  plane_terms(z0 + 1, A[2], B[2], C[2], ex, ey, ez);
-  for (int zo = z0; zo < z1; ++zo) {
+  // output plane zo from ring slots (i0, i1, i2) = planes (zo-1, zo, zo+1)
+  // and the newest plane zo+2, whose A/B/C then replace slot i0
+  auto step = [&](int zo, auto i0c, auto i1c, auto i2c) {
+    constexpr int i0 = decltype(i0c)::value, i1 = decltype(i1c)::value, i2 = decltype(i2c)::value;
     N a[2][2], b[2][2], c[2][2];
-    plane_terms(zo + 2, a, b, c, ex, ey, ez);
+    terms(a, b, c);
+    if (zo + 1 < z1) load(zo + 3);  // the next step's plane, in flight during this one
     float res[2][2];
 #pragma unroll
     for (int oy = 0; oy < 2; ++oy)
 #pragma unroll
       for (int ox = 0; ox < 2; ++ox) {
-        const N sxv = A[0][oy][ox] + 2 * A[1][oy][ox] + A[2][oy][ox] + ex[oy][ox];
-        const N syv = B[0][oy][ox] + 2 * B[1][oy][ox] + B[2][oy][ox] + ey[oy][ox];
-        const N szv = C[0][oy][ox] - C[2][oy][ox] + ez[oy][ox];
-        float fx = (float)sxv, fy = (float)syv, fz = (float)szv;
+        const N sxv = A[i0][oy][ox] + 2 * A[i1][oy][ox] + A[i2][oy][ox] + ex[oy][ox];
+        const N syv = B[i0][oy][ox] + 2 * B[i1][oy][ox] + B[i2][oy][ox] + ey[oy][ox];
+        const N szv = C[i0][oy][ox] - C[i2][oy][ox] + ez[oy][ox];
+        float fx = exact_float(sxv), fy = exact_float(syv), fz = exact_float(szv);
         if constexpr (WRAP) {
           float kx = 12.f, ky = 12.f, kz = 9.f;
           if (zflags & 0xFu) {  // a zero pixel in planes zo-1 .. zo+2: count exactly
@@ -141,7 +208,7 @@ __global__ void __launch_bounds__(SBX * SBY) k_sobel3d_fast(const S* __restrict_
           fy = fmaf(ky, 4294967296.0f, fy);
           fz = fmaf(kz, 4294967296.0f, fz);
         }
-        res[oy][ox] = sqrtf(fmaf(fx, fx, fmaf(fy, fy, fz * fz)));
+        res[oy][ox] = sqrt_approx(fmaf(fx, fx, fmaf(fy, fy, fz * fz)));
       }
 #pragma unroll
     for (int oy = 0; oy < 2; ++oy) {
@@ -152,11 +219,23 @@ __global__ void __launch_bounds__(SBX * SBY) k_sobel3d_fast(const S* __restrict_
 #pragma unroll
     for (int oy = 0; oy < 2; ++oy)
 #pragma unroll
-      for (int ox = 0; ox < 2; ++ox) {
-        A[0][oy][ox] = A[1][oy][ox], A[1][oy][ox] = A[2][oy][ox], A[2][oy][ox] = a[oy][ox];
-        B[0][oy][ox] = B[1][oy][ox], B[1][oy][ox] = B[2][oy][ox], B[2][oy][ox] = b[oy][ox];
-        C[0][oy][ox] = C[1][oy][ox], C[1][oy][ox] = C[2][oy][ox], C[2][oy][ox] = c[oy][ox];
-      }
+      for (int ox = 0; ox < 2; ++ox) A[i0][oy][ox] = a[oy][ox], B[i0][oy][ox] = b[oy][ox], C[i0][oy][ox] = c[oy][ox];
+  };
+
+  load(z0 - 1);
+  terms(A[0], B[0], C[0]);
+  load(z0);
+  terms(A[1], B[1], C[1]);
+  load(z0 + 1);
+  terms(A[2], B[2], C[2]);
+  load(z0 + 2);
+  using I0 = std::integral_constant<int, 0>;
+  using I1 = std::integral_constant<int, 1>;
+  using I2 = std::integral_constant<int, 2>;
+  for (int zo = z0; zo < z1; zo += 3) {  // unrolled by the ring length: slots rotate at compile time
+    step(zo, I0{}, I1{}, I2{});
+    if (zo + 1 < z1) step(zo + 1, I1{}, I2{}, I0{});
+    if (zo + 2 < z1) step(zo + 2, I2{}, I0{}, I1{});
   }
 }
 
@@ -180,7 +259,7 @@ template <class S, bool WRAP> clk_status launch_sobel(const Image& dst, const Im
 clk_status fast_sobel(const Image& dst, const Image& src, const Policy& p, cudaStream_t st) {
   if (src.ndim != 3 || dst.dt != CLK_F32 || src.w % 2 != 0 || src.w != dst.w || src.h != dst.h || src.d != dst.d)
     return CLK_UNSUPPORTED_DTYPE;
-  if ((uintptr_t)dst.ptr % 8 != 0) return CLK_UNSUPPORTED_DTYPE;
+  if ((uintptr_t)dst.ptr % 8 != 0 || (uintptr_t)src.ptr % (2 * dtype_size(src.dt)) != 0) return CLK_UNSUPPORTED_DTYPE;
   const bool wrap = !p.sobel_narrow;
   switch (src.dt) {
     case CLK_U16: return wrap ? launch_sobel<uint16_t, true>(dst, src, st) : launch_sobel<uint16_t, false>(dst, src, st);

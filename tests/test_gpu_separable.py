@@ -40,7 +40,10 @@ def close(got, val, scale):
 @pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.int8])
 def test_integer_isotropic_radii(clk, oracle, kernel, dt):
     rng = np.random.default_rng(31)
-    for shp in ((19, 70, 130), (3, 33, 64), (1, 40, 66), (40, 8, 10), (6, 29, 67), (2, 9, 1)):
+    # widths that are multiples of 16 take the vector staging (8/16-byte
+    # loads, clamped vectors at the tile borders); the others the scalar one
+    for shp in ((19, 70, 130), (3, 33, 64), (1, 40, 66), (40, 8, 10), (6, 29, 67), (2, 9, 1), (5, 37, 96),
+                (4, 20, 16), (3, 70, 208)):
         a = random_image(rng, shp, dt)
         for R in range(1, 9):
             for rz in (0, 1, R):
@@ -53,7 +56,7 @@ def test_integer_isotropic_radii(clk, oracle, kernel, dt):
 @pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.float32])
 def test_gaussian_to_float_isotropic(clk, oracle, dt):
     rng = np.random.default_rng(32)
-    for shp in ((17, 70, 130), (2, 35, 64), (5, 23, 45)):
+    for shp in ((17, 70, 130), (2, 35, 64), (5, 23, 45), (6, 40, 96), (3, 19, 16), (4, 45, 144)):
         a = random_image(rng, shp, dt)
         for R in (1, 3, 6, 9, 12):
             sig = R / 3.0
