@@ -367,7 +367,8 @@ def run_large(args):
 
     torch.cuda.set_device(0)
     peak, peak_kind = hbm_peak()
-    img = synth.blobs(LARGE_SHAPE, N_BLOBS, seed=SEED + 5, dtype=torch.float32, poisson=False, noise_sigma=20.0)
+    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else LARGE_SHAPE
+    img = synth.blobs(shape, N_BLOBS, seed=SEED + 5, dtype=torch.float32, poisson=False, noise_sigma=20.0)
     V = img.numel()
     out = torch.empty_like(img)
     stream = torch.cuda.current_stream()
@@ -379,6 +380,9 @@ def run_large(args):
         ("median_sphere r2", lambda: clk.execute("median_sphere_3d", {"src": img, "dst": out, "Nx": 5, "Ny": 5,
                                                                        "Nz": 5}, stream=stream)),
     ]
+    if args.filters:
+        import re
+        spec = [t for t in spec if re.search(args.filters, t[0])]
     for _ in range(max(3, args.warmup)):
         for _, fn in spec:
             fn()
@@ -412,7 +416,8 @@ def run_large(args):
         "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(total_ms / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded blob stack plus N(0,20) noise, float32",
-        "config": {"workload": "large-halo filters on 2048x2048x400 float32, each its own call", "voxels": V,
+        "config": {"workload": f"large-halo filters on {shape[2]}x{shape[1]}x{shape[0]} float32, each its own call",
+                   "voxels": V,
                    "l2": "inputs larger than L2 (6.7 GB); no flush"},
         "per_filter": per,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(dom_gbs, 1), "peak": peak, "unit": "GB/s",

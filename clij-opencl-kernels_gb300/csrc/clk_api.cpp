@@ -280,6 +280,13 @@ int slot_of(const KernelInfo& k, const char* nm) {
 
 clk_status device_ready_public() { return device_ready(); }
 
+clk_status sep_pass(SepOp op, const Image& dst, const Image& src, int axis, const SepTaps& taps, Range r,
+                    const Policy& pol, cudaStream_t st) {
+  const clk_status ls = line_pass(op, dst, src, axis, taps, pol, st);
+  if (ls != CLK_UNSUPPORTED_DTYPE) return ls;
+  return direct_sep_pass(op, dst, src, axis, taps, r, pol, st);
+}
+
 int* wait_flag_device() { return g_wait_flag_dev; }
 
 clk_status separable_plan(const char* kernel_name, const clk_image* dst_img, const clk_image* src_img,
@@ -461,7 +468,7 @@ clk_status clk_separable(const char* kernel_name, const clk_image* dst_img, cons
     const bool last = d == k->ndim - 1;
     Image out = dst;
     if (!last) out.ptr = tmp[d & 1];
-    st = skip[d] ? direct_copy(out, cur, r, pol, stm) : direct_sep_pass(op, out, cur, d, taps[d], r, pol, stm);
+    st = skip[d] ? direct_copy(out, cur, r, pol, stm) : sep_pass(op, out, cur, d, taps[d], r, pol, stm);
     cur = out;
   }
   for (int i = 0; i < 2; ++i)

@@ -325,7 +325,9 @@ ImgStep plan_sep(clk_batch* b, int s, int i, SepDesc* d) {
       return h;
     }
   }
-  // the generic fused kernel
+  // the generic fused kernel (where the plain path takes line passes, a
+  // plain call keeps parity)
+  if (prefer_line((SepOp)opn, out, in, ft.c, plan.pol)) return h;
   if (fused::fused_smem(cx, cy, cz, dtype_size(in.dt), dtype_size(out.dt)) > 200 * 1024) return h;
   d->algo = fast ? A_FUSED_FAST : A_FUSED_EXACT;
   h.algo = d->algo;

@@ -101,6 +101,25 @@ clk_status direct_sobel(const Image& dst, const Image& src, Range r, const Polic
 
 // ---- fused / tiled fast paths.  Return CLK_UNSUPPORTED_DTYPE (without
 // setting an error) when the case is not covered, so the caller falls back.
+// One separable pass along `axis` by the line kernels (clk_line.cu):
+// min/max of any pixel type (src type == dst type), mean of integer pixels,
+// Gaussian to float; radius 1..127.  CLK_UNSUPPORTED_DTYPE otherwise.
+bool line_eligible(SepOp op, const Image& dst, const Image& src, const Policy& pol);
+clk_status line_pass(SepOp op, const Image& dst, const Image& src, int axis, const SepTaps& taps, const Policy& pol,
+                     cudaStream_t st);
+// Whole-filter routing shared by clk_separable and the batch planner: a
+// filter the register-window kernels cannot take runs as line passes (one
+// launch per axis) rather than the generic fused kernel once a radius
+// exceeds this.
+constexpr int kLineMinR = 12;
+inline bool prefer_line(SepOp op, const Image& dst, const Image& src, const int c[3], const Policy& pol) {
+  const int m = c[0] > c[1] ? (c[0] > c[2] ? c[0] : c[2]) : (c[1] > c[2] ? c[1] : c[2]);
+  return m > kLineMinR && line_eligible(op, dst, src, pol);
+}
+// the separable pass the multi-pass orchestration runs for one axis: a
+// line pass where eligible, else the reference-order generic kernel
+clk_status sep_pass(SepOp op, const Image& dst, const Image& src, int axis, const SepTaps& taps, Range r,
+                    const Policy& pol, cudaStream_t st);
 clk_status fused_separable(SepOp op, const Image& dst, const Image& src, const SepTaps taps[3], const bool skip[3],
                            const Policy& p, cudaStream_t st);
 clk_status fast_morph(bool erode, bool sphere, int iterations, const Image& dst, const Image& src, const Policy& p,

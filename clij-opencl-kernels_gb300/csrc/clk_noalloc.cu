@@ -85,7 +85,7 @@ extern "C" clk_status clk_separable_noalloc(const char* kernel_name, const clk_i
     Image out = plan.dst;
     if (d != plan.ndim - 1) out.ptr = tmp[d & 1];
     st = plan.skip[d] ? direct_copy(out, cur, r, plan.pol, stm)
-                      : direct_sep_pass(plan.op, out, cur, d, plan.taps[d], r, plan.pol, stm);
+                      : sep_pass(plan.op, out, cur, d, plan.taps[d], r, plan.pol, stm);
     cur = out;
   }
   return st;

@@ -74,7 +74,10 @@ template <class S, int OP, int R, int MODE = STAGE_SCALAR> struct Geo {
   static constexpr int NWD = rnd((XOFF + WIN_X) * ES, XV) / 4;
   static constexpr size_t buf_bytes() { return ((size_t)NEL * sizeof(S) + 127) & ~size_t(127); }
   static constexpr size_t tin_bytes() { return NBUF * buf_bytes(); }
-  static constexpr size_t xs_bytes() { return ((size_t)RH * TX * sizeof(T) + 15) & ~size_t(15); }
+  // X-pass results, row pitch XP: padded so that the X pass's stores (a warp
+  // = 4 row pairs x 8 segments) spread over the banks
+  static constexpr int XP = TX + (sizeof(T) == 2 ? 2 : 4);
+  static constexpr size_t xs_bytes() { return ((size_t)RH * XP * sizeof(T) + 15) & ~size_t(15); }
   static __host__ __device__ size_t ring_bytes(int cz) { return (size_t)(2 * cz + 1) * TY * TX * sizeof(T); }
   static size_t smem(int cz) { return tin_bytes() + xs_bytes() + ring_bytes(cz); }
 };
@@ -320,23 +323,24 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
       __syncthreads();
     }
 
-    // ---------------- X pass: rows (2rp, 2rp+1) x outputs sg*SEGX ..
+    // ---------------- X pass: rows (rp, rp + RH/2) x outputs sg*SEGX ..
     {
       const int rp = tid / (TX / SEGX), sg = tid % (TX / SEGX);
-      if (rp < G::RH / 2) {
-        const S* r0 = tcur + (2 * rp) * G::RW + sg * SEGX + XOFF;
-        const S* r1 = r0 + G::RW;
-        T* o0 = xs + (2 * rp) * TX + sg * SEGX;
-        T* o1 = o0 + TX;
+      constexpr int HALF = G::RH / 2;
+      if (rp < HALF) {
+        const S* r0 = tcur + rp * G::RW + sg * SEGX + XOFF;
+        const S* r1 = r0 + HALF * G::RW;
+        T* o0 = xs + rp * G::XP + sg * SEGX;
+        T* o1 = o0 + HALF * G::XP;
         // aligned stagings: the segment's words of both rows, read as vectors
         uint32_t w0[MODE == STAGE_SCALAR ? 1 : G::NWD], w1[MODE == STAGE_SCALAR ? 1 : G::NWD];
         if constexpr (MODE != STAGE_SCALAR) {
-          const S* a0 = tcur + (2 * rp) * G::RW + sg * SEGX;
+          const S* a0 = tcur + rp * G::RW + sg * SEGX;
           if constexpr (G::XV == 16) {
 #pragma unroll
             for (int v = 0; v < G::NWD / 4; ++v) {
               const uint4 x = reinterpret_cast<const uint4*>(a0)[v];
-              const uint4 y = reinterpret_cast<const uint4*>(a0 + G::RW)[v];
+              const uint4 y = reinterpret_cast<const uint4*>(a0 + HALF * G::RW)[v];
               w0[4 * v] = x.x, w0[4 * v + 1] = x.y, w0[4 * v + 2] = x.z, w0[4 * v + 3] = x.w;
               w1[4 * v] = y.x, w1[4 * v + 1] = y.y, w1[4 * v + 2] = y.z, w1[4 * v + 3] = y.w;
             }
@@ -344,7 +348,7 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
 #pragma unroll
             for (int v = 0; v < G::NWD / 2; ++v) {
               const uint2 x = reinterpret_cast<const uint2*>(a0)[v];
-              const uint2 y = reinterpret_cast<const uint2*>(a0 + G::RW)[v];
+              const uint2 y = reinterpret_cast<const uint2*>(a0 + HALF * G::RW)[v];
               w0[2 * v] = x.x, w0[2 * v + 1] = x.y;
               w1[2 * v] = y.x, w1[2 * v + 1] = y.y;
             }
@@ -424,12 +428,12 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
     // ---------------- Y pass: column pair cp x rows sy*SEGY .. -> ring slot
     T* rs = ring + (size_t)wslot * TY * TX;
     {
-      const T* col = xs + (sy * SEGY) * TX + 2 * cp;
+      const T* col = xs + (sy * SEGY) * G::XP + 2 * cp;
       T* o = rs + (sy * SEGY) * TX + 2 * cp;
       if constexpr (OP == MIN || OP == MAX) {
         uint32_t win[G::WIN_Y];
 #pragma unroll
-        for (int k = 0; k < G::WIN_Y; ++k) win[k] = *reinterpret_cast<const uint32_t*>(col + k * TX);
+        for (int k = 0; k < G::WIN_Y; ++k) win[k] = *reinterpret_cast<const uint32_t*>(col + k * G::XP);
         uint32_t out[SEGY];
         window_minmax<S, OP, SEGY, R>(win, out);
 #pragma unroll
@@ -437,7 +441,7 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
       } else if constexpr (OP == MEAN) {
         int w0[G::WIN_Y], w1[G::WIN_Y];
 #pragma unroll
-        for (int k = 0; k < G::WIN_Y; ++k) w0[k] = (int)col[k * TX], w1[k] = (int)col[k * TX + 1];
+        for (int k = 0; k < G::WIN_Y; ++k) w0[k] = (int)col[k * G::XP], w1[k] = (int)col[k * G::XP + 1];
         int s0 = 0, s1 = 0;
 #pragma unroll
         for (int k = 0; k <= 2 * R; ++k) s0 += w0[k], s1 += w1[k];
@@ -455,7 +459,7 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
       } else {
         uint64_t win[G::WIN_Y];
 #pragma unroll
-        for (int k = 0; k < G::WIN_Y; ++k) win[k] = *reinterpret_cast<const uint64_t*>(col + k * TX);
+        for (int k = 0; k < G::WIN_Y; ++k) win[k] = *reinterpret_cast<const uint64_t*>(col + k * G::XP);
 #pragma unroll
         for (int j = 0; j < SEGY; ++j) {
           uint64_t acc = f2_fma(f2_bcast(p.wy[0]), win[j + R], 0ull);
@@ -561,11 +565,12 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
   }
 }
 
-// CTAs per SM the register budget is sized for (85 / 128 registers)
-template <int OP> constexpr int min_ctas() { return OP == GAUSS ? 2 : 3; }
+// CTAs per SM the register budget is sized for (64 / 80 / 128 registers;
+// the vector staging holds fewer prefetch registers than the scalar one)
+template <int OP, int MODE> constexpr int min_ctas() { return OP == GAUSS ? 2 : MODE == STAGE_VEC ? 4 : 3; }
 
 template <class S, class D, int OP, int R, int MODE>
-__global__ void __launch_bounds__(NT, min_ctas<OP>()) k_sep2(const S* __restrict__ src, D* __restrict__ dst, int W,
+__global__ void __launch_bounds__(NT, min_ctas<OP, MODE>()) k_sep2(const S* __restrict__ src, D* __restrict__ dst, int W,
                                                              int H, int Dz, int zchunk,
                                                              const __grid_constant__ Params p) {
   extern __shared__ __align__(128) unsigned char smem[];

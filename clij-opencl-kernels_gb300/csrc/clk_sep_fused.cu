@@ -129,6 +129,7 @@ clk_status fused_separable(SepOp op, const Image& dst, const Image& src, const S
     }
     if (s2 != CLK_UNSUPPORTED_DTYPE) return s2;
   }
+  if (prefer_line(op, dst, src, ft.c, p)) return CLK_UNSUPPORTED_DTYPE;  // the caller chains line passes
   if (fused_smem(ft.c[0], ft.c[1], ft.c[2], dtype_size(src.dt), dtype_size(dst.dt)) > 200 * 1024)
     return CLK_UNSUPPORTED_DTYPE;
   const int s = src.dt, d = dst.dt;
