@@ -40,6 +40,15 @@ SAMPLE = (32, 256, 256)  # CPU-baseline sample: a sub-stack of the same data
 METRIC = "Gvoxel/s (plain filter suite, 1024x1024x256)"
 
 
+# DRAM bytes per voxel (read + write) of each filter's kernel from the ncu
+# capture summarised in profiles/sep2_sobel_median_kernels_1024x1024x128_u16.md
+# (a 1024x1024x128 slab of the same stack; traffic scales with the voxels).
+NCU_DRAM_BYTES_PER_VOXEL = {
+    "gaussian_blur s(3,3,1.5)": 5.88, "mean_box r(5,5,2)": 3.95, "minimum_box r(5,5,2)": 3.98,
+    "median_box r1": 3.74, "median_sphere r2": 3.74, "sobel_3d": 5.66,
+}
+
+
 def suite_spec():
     """(name, kind, kernel, params, src, dst dtype code, bytes/voxel)."""
     return [
@@ -512,17 +521,18 @@ def main():
     tmp_mask = torch.empty_like(mask)
     stream = torch.cuda.current_stream()
 
-    def run(name, kind, kernel, params, srcn, src_t, out_t):
+    def run(name, kind, kernel, params, srcn, src_t, out_t, st=None):
+        st = stream if st is None else st
         if kind == "sep":
-            clk.separable(kernel, src_t, out_t, params[0], params[1], stream=stream)
+            clk.separable(kernel, src_t, out_t, params[0], params[1], stream=st)
         elif kind == "exec":
             p = {"src": src_t, "dst": out_t}
             p.update(params)
-            clk.execute(kernel, p, stream=stream)
+            clk.execute(kernel, p, stream=st)
         elif params == 1:  # r=1: one launch of the reference kernel
-            clk.execute(kernel, {"src": src_t, "dst": out_t}, stream=stream)
+            clk.execute(kernel, {"src": src_t, "dst": out_t}, stream=st)
         else:  # radius r: r successive launches, fused in pairs
-            clk.morphology(kernel, src_t, out_t, params, stream=stream)
+            clk.morphology(kernel, src_t, out_t, params, stream=st)
 
     def step(srcs):
         for name, kind, kernel, params, srcn, ddt, bpv in spec:
@@ -567,29 +577,58 @@ def main():
 
     e2e = None
     if not args.no_e2e:
+        # The same suite from pinned host buffers, pipelined the way a caller
+        # would: host->device copies of step k+1, the filters of step k and
+        # device->host copies of step k's outputs run on three streams, with
+        # two sets of device buffers.  Every byte still crosses the link.
         h_img = img.cpu().pin_memory()
         h_mask = mask.cpu().pin_memory()
         h_out = {n: torch.empty(shape, dtype=o.dtype).pin_memory() for n, o in outs.items()}
-        d_img, d_mask = torch.empty_like(img), torch.empty_like(mask)
+        d_in = [{"img": torch.empty_like(img), "mask": torch.empty_like(mask)} for _ in range(2)]
+        d_out = [{n: torch.empty_like(o) for n, o in outs.items()} for _ in range(2)]
+        cs, hs, ds = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+        ev_in = [torch.cuda.Event() for _ in range(2)]
+        ev_in_free = [torch.cuda.Event() for _ in range(2)]
+        ev_out = [{n: torch.cuda.Event() for n in outs} for _ in range(2)]
+        ev_out_free = [{n: torch.cuda.Event() for n in outs} for _ in range(2)]
+        used = [False, False]
 
-        def e2e_step():
-            d_img.copy_(h_img, non_blocking=True)
-            d_mask.copy_(h_mask, non_blocking=True)
-            step({"img": d_img, "mask": d_mask})
-            for n, o in outs.items():
-                h_out[n].copy_(o, non_blocking=True)
+        def e2e_step(k):
+            b = k % 2
+            with torch.cuda.stream(hs):
+                if used[b]:
+                    hs.wait_event(ev_in_free[b])
+                d_in[b]["img"].copy_(h_img, non_blocking=True)
+                d_in[b]["mask"].copy_(h_mask, non_blocking=True)
+                ev_in[b].record(hs)
+            cs.wait_event(ev_in[b])
+            for name, kind, kernel, params, srcn, ddt, bpv in spec:
+                if used[b]:
+                    cs.wait_event(ev_out_free[b][name])
+                run(name, kind, kernel, params, srcn, d_in[b][srcn], d_out[b][name], st=cs)
+                ev_out[b][name].record(cs)
+            ev_in_free[b].record(cs)
+            with torch.cuda.stream(ds):
+                for name in outs:
+                    ds.wait_event(ev_out[b][name])
+                    h_out[name].copy_(d_out[b][name], non_blocking=True)
+                    ev_out_free[b][name].record(ds)
+            used[b] = True
 
-        e2e_step()
+        e2e_step(0)
+        e2e_step(1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step()
+        for k in range(args.steps):
+            e2e_step(k)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         e2e = {"value": round(V * len(spec) * args.steps / dt / 1e9, 3), "unit": "Gvoxel/s",
                "h2d_bytes_per_step": img.numel() * 2 + mask.numel(),
                "d2h_bytes_per_step": sum(o.numel() * o.element_size() for o in outs.values()),
-               "path": "pinned host stack + mask -> device, clk C-ABI calls, all outputs -> pinned host"}
+               "ms_per_step": round(dt * 1e3 / args.steps, 2),
+               "path": "pinned host stack + mask -> device, clk C-ABI calls, all outputs -> pinned host; "
+                       "copies and filters pipelined on three streams"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -612,7 +651,9 @@ def main():
             "per_filter": per,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(dom_gbs, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(dom_gbs / peak, 4), "peak_kind": peak_kind,
-                         "traffic": None},
+                         "traffic": (round(NCU_DRAM_BYTES_PER_VOXEL[dom] * V) if dom in NCU_DRAM_BYTES_PER_VOXEL
+                                     else None),
+                         "algorithmic_bytes": int(V * per[dom]["bytes_per_voxel"])},
             "gpu_launches": launches,
             "clocks": clocks.result,
             "e2e": e2e,

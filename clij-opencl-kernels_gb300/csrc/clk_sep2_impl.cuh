@@ -48,7 +48,7 @@ enum Stage {
 // RA >= R elements left of the tile, RA rounded up so that every staged
 // vector (TMA: the box origin) is aligned; the X pass then reads from column
 // RA - R.
-template <class S, int OP, int R, int MODE = STAGE_SCALAR> struct Geo {
+template <class S, int OP, int R, int MODE = STAGE_SCALAR, bool PIPE = false> struct Geo {
   typedef typename Temp<S, OP>::T T;
   static constexpr int ES = (int)sizeof(S);
   static constexpr int rnd(int v, int m) { return (v + m - 1) / m * m; }
@@ -64,7 +64,8 @@ template <class S, int OP, int R, int MODE = STAGE_SCALAR> struct Geo {
   static constexpr int SR = RW / VE;          // staging vectors per row
   static constexpr int NSLOT = RH * SR;
   static constexpr int PERV = (NSLOT + NT - 1) / NT;
-  static constexpr int NBUF = MODE == STAGE_TMA ? 2 : 1;
+  static constexpr int NBUF = (MODE == STAGE_TMA || PIPE) ? 2 : 1;  // staged tiles
+  static constexpr int NXS = PIPE ? 2 : 1;                            // X-pass result buffers
   static constexpr int WIN_X = SEGX + 2 * R;
   static constexpr int WIN_Y = SEGY + 2 * R;
   static constexpr int XOFF = RA - R;         // first staged column the X pass reads
@@ -79,7 +80,7 @@ template <class S, int OP, int R, int MODE = STAGE_SCALAR> struct Geo {
   static constexpr int XP = TX + (sizeof(T) == 2 ? 2 : 4);
   static constexpr size_t xs_bytes() { return ((size_t)RH * XP * sizeof(T) + 15) & ~size_t(15); }
   static __host__ __device__ size_t ring_bytes(int cz) { return (size_t)(2 * cz + 1) * TY * TX * sizeof(T); }
-  static size_t smem(int cz) { return tin_bytes() + xs_bytes() + ring_bytes(cz); }
+  static size_t smem(int cz) { return tin_bytes() + NXS * xs_bytes() + ring_bytes(cz); }
 };
 
 // ---------------------------------------------------------------- words
@@ -182,17 +183,20 @@ __device__ __forceinline__ void window_minmax(const uint32_t (&win)[M + 2 * R], 
 // aligned).  TMA: map is a 3-D tensor map of src with a (RW, RH, 1) box;
 // err receives 1 if a bounded wait for a tile ran out (the tile is then
 // abandoned).
-template <class S, class D, int OP, int R, int MODE = STAGE_SCALAR>
+template <class S, class D, int OP, int R, int MODE = STAGE_SCALAR, bool PIPE = false>
 __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restrict__ dst, int W, int H, int Dz,
                                           int zchunk, const Params& p, int bx, int by, int bz,
                                           unsigned char* smem, const CUtensorMap* map = nullptr,
                                           int* err = nullptr) {
-  using G = Geo<S, OP, R, MODE>;
+  using G = Geo<S, OP, R, MODE, PIPE>;
   using T = typename G::T;
   constexpr bool TMA = MODE == STAGE_TMA;
+  static_assert(!(TMA && PIPE), "the pipelined loop stages from registers");
   S* tin = reinterpret_cast<S*>(smem);
   T* xs = reinterpret_cast<T*>(smem + G::tin_bytes());
-  T* ring = reinterpret_cast<T*>(smem + G::tin_bytes() + G::xs_bytes());
+  T* ring = reinterpret_cast<T*>(smem + G::tin_bytes() + G::NXS * G::xs_bytes());
+  auto tinb = [&](int b) { return reinterpret_cast<S*>(smem + b * G::buf_bytes()); };
+  auto xsb = [&](int b) { return reinterpret_cast<T*>(smem + G::tin_bytes() + b * G::xs_bytes()); };
   const int cz = p.cz, NZ = 2 * cz + 1;
   const int tid = threadIdx.x;
   const int x0 = bx * TX, y0 = by * TY;
@@ -237,18 +241,18 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
       }
     }
   };
-  auto commit = [&]() {
+  auto commit = [&](S* to) {
     if constexpr (MODE == STAGE_SCALAR) {
 #pragma unroll
       for (int k = 0; k < G::PER; ++k) {
         const int i = tid + k * NT;
-        if (i < G::NEL) tin[i] = pre[k];
+        if (i < G::NEL) to[i] = pre[k];
       }
     } else if constexpr (MODE == STAGE_VEC) {
 #pragma unroll
       for (int k = 0; k < G::PERV; ++k) {
         const int sl = tid + k * NT;
-        if (k < G::PERV - 1 || sl < G::NSLOT) reinterpret_cast<VT*>(tin)[sl] = prev[k];
+        if (k < G::PERV - 1 || sl < G::NSLOT) reinterpret_cast<VT*>(to)[sl] = prev[k];
       }
     }
   };
@@ -298,31 +302,8 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
   int zs0[SEGY], zs1[SEGY];  // mean: running sums along z of this thread's cells
 #pragma unroll
   for (int j = 0; j < SEGY; ++j) zs0[j] = zs1[j] = 0;
-  for (int zi = z0 - cz, it = 0; zi < z1 + cz; ++zi, ++it) {
-    S* tcur = tin;
-    if constexpr (TMA) {
-      const int buf = it & 1;
-      tcur = reinterpret_cast<S*>(reinterpret_cast<unsigned char*>(tin) + buf * G::buf_bytes());
-      if (tid == 0) stalled = tma::mbar_wait(&bars[buf], (it >> 1) & 1) ? 0 : 1;
-      __syncthreads();  // tile landed; previous Y pass done with xs
-      if (stalled) {    // the copy never arrived: report, drain the other buffer, give up on this tile
-        if (tid == 0) {
-          if (err) atomicExch(err, 1);
-          if (zi + 1 < z1 + cz) tma::mbar_wait(&bars[buf ^ 1], ((it + 1) >> 1) & 1);
-        }
-        return;
-      }
-      if (border) {
-        fix_border(tcur);
-        __syncthreads();
-      }
-    } else {  // scalar / vector staging from the register prefetch
-      __syncthreads();  // previous X pass done with tin, previous Y pass with xs
-      commit();
-      if (zi + 1 < z1 + cz) fetch(zi + 1);
-      __syncthreads();
-    }
-
+  // X pass of the staged tile tcur into the X-result buffer xs
+  auto xpass = [&](const S* tcur, T* xs) {
     // ---------------- X pass: rows (rp, rp + RH/2) x outputs sg*SEGX ..
     {
       const int rp = tid / (TX / SEGX), sg = tid % (TX / SEGX);
@@ -417,14 +398,10 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
         }
       }
     }
-    if constexpr (TMA) {
-      if (border) tma::fence_proxy_async();  // this thread's fix-up writes of tcur before the refill
-    }
-    __syncthreads();
-    if constexpr (TMA) {
-      if (tid == 0 && zi + 2 < z1 + cz) issue(zi + 2, it & 1);
-    }
-
+  };
+  // Y pass of the X results xs of plane zi into the ring, then the Z pass
+  // of the output plane zi - cz
+  auto yzpass = [&](const T* xs, int zi) {
     // ---------------- Y pass: column pair cp x rows sy*SEGY .. -> ring slot
     T* rs = ring + (size_t)wslot * TY * TX;
     {
@@ -562,6 +539,63 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
         }
       }
     }
+  };
+
+  if constexpr (PIPE) {
+    // One barrier per plane: the staged tile and the X results are double
+    // buffered, so the X pass of plane i runs in the same phase as the Y/Z
+    // passes of plane i-1 (threads idle in the X pass go on to Y/Z).
+    const int NPL = z1 + 2 * cz - z0;  // planes z0-cz .. z1+cz-1
+    commit(tinb(0));
+    if (NPL > 1) fetch(z0 - cz + 1);
+    __syncthreads();
+    for (int it = 0; it <= NPL; ++it) {
+      const int zi = z0 - cz + it;
+      if (it < NPL) {
+        if (it + 1 < NPL) {
+          commit(tinb((it + 1) & 1));
+          if (it + 2 < NPL) fetch(zi + 2);
+        }
+        xpass(tinb(it & 1), xsb(it & 1));
+      }
+      if (it >= 1) yzpass(xsb((it - 1) & 1), zi - 1);
+      __syncthreads();
+    }
+  } else {
+    for (int zi = z0 - cz, it = 0; zi < z1 + cz; ++zi, ++it) {
+      S* tcur = tin;
+      if constexpr (TMA) {
+        const int buf = it & 1;
+        tcur = reinterpret_cast<S*>(reinterpret_cast<unsigned char*>(tin) + buf * G::buf_bytes());
+        if (tid == 0) stalled = tma::mbar_wait(&bars[buf], (it >> 1) & 1) ? 0 : 1;
+        __syncthreads();  // tile landed; previous Y pass done with xs
+        if (stalled) {    // the copy never arrived: report, drain the other buffer, give up on this tile
+          if (tid == 0) {
+            if (err) atomicExch(err, 1);
+            if (zi + 1 < z1 + cz) tma::mbar_wait(&bars[buf ^ 1], ((it + 1) >> 1) & 1);
+          }
+          return;
+        }
+        if (border) {
+          fix_border(tcur);
+          __syncthreads();
+        }
+      } else {  // scalar / vector staging from the register prefetch
+        __syncthreads();  // previous X pass done with tin, previous Y pass with xs
+        commit(tin);
+        if (zi + 1 < z1 + cz) fetch(zi + 1);
+        __syncthreads();
+      }
+      xpass(tcur, xs);
+      if constexpr (TMA) {
+        if (border) tma::fence_proxy_async();  // this thread's fix-up writes of tcur before the refill
+      }
+      __syncthreads();
+      if constexpr (TMA) {
+        if (tid == 0 && zi + 2 < z1 + cz) issue(zi + 2, it & 1);
+      }
+      yzpass(xs, zi);
+    }
   }
 }
 
@@ -569,12 +603,12 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
 // the vector staging holds fewer prefetch registers than the scalar one)
 template <int OP, int MODE> constexpr int min_ctas() { return OP == GAUSS ? 2 : MODE == STAGE_VEC ? 4 : 3; }
 
-template <class S, class D, int OP, int R, int MODE>
+template <class S, class D, int OP, int R, int MODE, bool PIPE = false>
 __global__ void __launch_bounds__(NT, min_ctas<OP, MODE>()) k_sep2(const S* __restrict__ src, D* __restrict__ dst, int W,
                                                              int H, int Dz, int zchunk,
                                                              const __grid_constant__ Params p) {
   extern __shared__ __align__(128) unsigned char smem[];
-  sep2_tile<S, D, OP, R, MODE>(src, dst, W, H, Dz, zchunk, p, blockIdx.x, blockIdx.y, blockIdx.z, smem);
+  sep2_tile<S, D, OP, R, MODE, PIPE>(src, dst, W, H, Dz, zchunk, p, blockIdx.x, blockIdx.y, blockIdx.z, smem);
 }
 
 // Same tile body with the halo tile staged by TMA, double-buffered: the copy
@@ -629,12 +663,15 @@ clk_status launch(const Image& dst, const Image& src, const Params& p, cudaStrea
     count_launch();
     return check_launch("separable (fused, sep2, tma)");
   }
-  // vector staging when the image base and rows are aligned to its vectors
-  using GV = Geo<S, OP, R, STAGE_VEC>;
+  // vector staging when the image base and rows are aligned to its vectors;
+  // the pipelined loop (double-buffered tiles, one barrier per plane) where
+  // its shared memory leaves several CTAs per SM: min / max / mean
+  constexpr bool PIPE = OP != GAUSS;
+  using GV = Geo<S, OP, R, STAGE_VEC, PIPE>;
   if ((uintptr_t)src.ptr % GV::SV == 0 && ((int64_t)src.w * (int64_t)sizeof(S)) % GV::SV == 0 &&
-      smem_ok(k_sep2<S, D, OP, R, STAGE_VEC>, GV::smem(p.cz))) {
-    k_sep2<S, D, OP, R, STAGE_VEC><<<grid, NT, GV::smem(p.cz), st>>>((const S*)src.ptr, (D*)dst.ptr, dst.w, dst.h,
-                                                                     dst.d, zchunk, p);
+      smem_ok(k_sep2<S, D, OP, R, STAGE_VEC, PIPE>, GV::smem(p.cz))) {
+    k_sep2<S, D, OP, R, STAGE_VEC, PIPE><<<grid, NT, GV::smem(p.cz), st>>>((const S*)src.ptr, (D*)dst.ptr, dst.w,
+                                                                           dst.h, dst.d, zchunk, p);
     count_launch();
     return check_launch("separable (fused, sep2, vector staging)");
   }

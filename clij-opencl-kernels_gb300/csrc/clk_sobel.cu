@@ -239,6 +239,186 @@ __global__ void __launch_bounds__(SBX * SBY, 2) k_sobel3d_fast(const S* __restri
   }
 }
 
+// The same computation with each input plane staged once in shared memory:
+// a CTA owns 64 x 16 outputs and streams along z; plane p+1 is fetched into
+// registers with 16-byte vector loads (vectors wholly outside a row take the
+// clamped edge pixel) while plane p is used, and two plane buffers need one
+// barrier per plane.  Requires rows of a whole number of vectors.
+constexpr int TSX = 64, TSY = 16;  // outputs per CTA; 32 x 8 threads of 2 x 2
+
+template <class S> __device__ __forceinline__ uint4 splat16(S v) {
+  uint32_t w;
+  if constexpr (sizeof(S) == 4) w = __float_as_uint(v);
+  else if constexpr (sizeof(S) == 2) w = (uint32_t)(uint16_t)v * 0x10001u;
+  else w = (uint32_t)(uint8_t)v * 0x01010101u;
+  return make_uint4(w, w, w, w);
+}
+
+template <class S, bool WRAP>
+__global__ void __launch_bounds__(256, WRAP ? 2 : 3) k_sobel3d_tile(const S* __restrict__ src, float* __restrict__ dst, int W,
+                                                         int H, int D, int zchunk) {
+  using N = typename Num<S>::type;
+  using PV = typename Pair<S>::V;
+  constexpr int VE = 16 / (int)sizeof(S);  // pixels per vector
+  constexpr int RA = VE;                   // staged columns x0 - RA .. x0 + 64 + RA - 1
+  constexpr int RW = TSX + 2 * RA, RH = TSY + 3;  // rows y0 - 1 .. y0 + 17
+  constexpr int SR = RW / VE, NSLOT = RH * SR, PERV = (NSLOT + 255) / 256;
+  __shared__ __align__(16) S tile[2][RH * RW];
+  const int tid = threadIdx.x, px = tid & 31, py = tid >> 5;
+  const int x0 = blockIdx.x * TSX, y0 = blockIdx.y * TSY;
+  const int x = x0 + 2 * px, y = y0 + 2 * py;
+  const bool act = x < W && y < H;
+  const int z0 = blockIdx.z * zchunk, z1 = min(D, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+
+  uint4 pre[PERV];
+  auto fetch = [&](int p) {
+    const S* sp = src + (int64_t)clampi(p, D - 1) * plane;
+#pragma unroll
+    for (int k = 0; k < PERV; ++k) {
+      const int sl = tid + k * 256;
+      if (sl < NSLOT) {
+        const int r = sl / SR, v = sl - r * SR;
+        const S* rowp = sp + (int64_t)clampi(y0 - 1 + r, H - 1) * W;
+        const int gx = x0 - RA + v * VE;
+        pre[k] = (gx >= 0 && gx < W) ? __ldg(reinterpret_cast<const uint4*>(rowp + gx))
+                                     : splat16<S>(__ldg(rowp + (gx < 0 ? 0 : W - 1)));
+      }
+    }
+  };
+  int pn = z0 - 1;  // the next plane to stage (its pixels are in pre)
+  PV raw[4][3];
+  // stage plane pn, start fetching pn + 1, and read this thread's pairs
+  auto next_plane = [&]() {
+    S* t = tile[(pn - z0 + 1) & 1];
+#pragma unroll
+    for (int k = 0; k < PERV; ++k) {
+      const int sl = tid + k * 256;
+      if (sl < NSLOT) reinterpret_cast<uint4*>(t)[sl] = pre[k];
+    }
+    if (pn + 1 <= z1 + 1) fetch(pn + 1);
+    ++pn;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const PV* row = reinterpret_cast<const PV*>(t + (2 * py + r) * RW + RA + 2 * px - 2);
+      raw[r][0] = row[0], raw[r][1] = row[1], raw[r][2] = row[2];
+    }
+  };
+
+  N A[3][2][2], B[3][2][2], C[3][2][2];
+  N ex[2][2], ey[2][2], ez[2][2];
+  uint32_t zflags = 0;
+  auto terms = [&](N (&a)[2][2], N (&b)[2][2], N (&c)[2][2]) {
+    N v[4][4];  // rows y-1 .. y+2, columns x-1 .. x+2 (clamped by the staging)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      v[r][0] = Pair<S>::hi(raw[r][0]);
+      v[r][1] = Pair<S>::lo(raw[r][1]);
+      v[r][2] = Pair<S>::hi(raw[r][1]);
+      v[r][3] = Pair<S>::lo(raw[r][2]);
+    }
+    if constexpr (WRAP) {
+      N m = v[0][0];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) m = min(m, v[r][c]);
+      zflags = (zflags << 1) | (m == 0 ? 1u : 0u);
+    }
+    N sx[4][2], dx[4][2];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int o = 0; o < 2; ++o) {
+        sx[r][o] = v[r][o] + 2 * v[r][o + 1] + v[r][o + 2];
+        dx[r][o] = v[r][o] - v[r][o + 2];
+      }
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) {
+        const int rm = oy, rc = oy + 1, rp = oy + 2;
+        a[oy][ox] = dx[rm][ox] + 2 * dx[rc][ox] + dx[rp][ox];
+        b[oy][ox] = sx[rm][ox] - sx[rp][ox];
+        c[oy][ox] = sx[rm][ox] + 2 * sx[rc][ox] + sx[rp][ox];
+        const N q = 2 * v[rp][ox] + v[rp][ox + 1];
+        ex[oy][ox] = 2 * dx[rm][ox] + dx[rc][ox] - v[rp][ox + 1];
+        ey[oy][ox] = q - sx[rc][ox];
+        ez[oy][ox] = 2 * sx[rm][ox] + sx[rc][ox] + q;
+      }
+  };
+  auto step = [&](int zo, auto i0c, auto i1c, auto i2c) {
+    constexpr int i0 = decltype(i0c)::value, i1 = decltype(i1c)::value, i2 = decltype(i2c)::value;
+    N a[2][2], b[2][2], c[2][2];
+    next_plane();  // plane zo + 2
+    terms(a, b, c);
+    float res[2][2];
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) {
+        const N sxv = A[i0][oy][ox] + 2 * A[i1][oy][ox] + A[i2][oy][ox] + ex[oy][ox];
+        const N syv = B[i0][oy][ox] + 2 * B[i1][oy][ox] + B[i2][oy][ox] + ey[oy][ox];
+        const N szv = C[i0][oy][ox] - C[i2][oy][ox] + ez[oy][ox];
+        float fx = exact_float(sxv), fy = exact_float(syv), fz = exact_float(szv);
+        if constexpr (WRAP) {
+          float kx = 12.f, ky = 12.f, kz = 9.f;
+          if ((zflags & 0xFu) && act) {  // a zero pixel in planes zo-1 .. zo+2: count exactly
+            const float3 k = wrap_counts<S>(src, W, H, D, x + ox, y + oy, zo);
+            kx = k.x, ky = k.y, kz = k.z;
+          }
+          fx = fmaf(kx, 4294967296.0f, fx);
+          fy = fmaf(ky, 4294967296.0f, fy);
+          fz = fmaf(kz, 4294967296.0f, fz);
+        }
+        res[oy][ox] = sqrt_approx(fmaf(fx, fx, fmaf(fy, fy, fz * fz)));
+      }
+    if (act) {
+#pragma unroll
+      for (int oy = 0; oy < 2; ++oy) {
+        if (y + oy < H)
+          *reinterpret_cast<float2*>(dst + (int64_t)zo * plane + (int64_t)(y + oy) * W + x) =
+              make_float2(res[oy][0], res[oy][1]);
+      }
+    }
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) A[i0][oy][ox] = a[oy][ox], B[i0][oy][ox] = b[oy][ox], C[i0][oy][ox] = c[oy][ox];
+  };
+
+  fetch(z0 - 1);
+  next_plane();
+  terms(A[0], B[0], C[0]);
+  next_plane();
+  terms(A[1], B[1], C[1]);
+  next_plane();
+  terms(A[2], B[2], C[2]);
+  using I0 = std::integral_constant<int, 0>;
+  using I1 = std::integral_constant<int, 1>;
+  using I2 = std::integral_constant<int, 2>;
+  for (int zo = z0; zo < z1; zo += 3) {
+    step(zo, I0{}, I1{}, I2{});
+    if (zo + 1 < z1) step(zo + 1, I1{}, I2{}, I0{});
+    if (zo + 2 < z1) step(zo + 2, I2{}, I0{}, I1{});
+  }
+}
+
+template <class S, bool WRAP> clk_status launch_sobel_tile(const Image& dst, const Image& src, cudaStream_t st) {
+  const int tx = (src.w + TSX - 1) / TSX, ty = (src.h + TSY - 1) / TSY;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int chunks = 1;
+  while ((int64_t)tx * ty * chunks < 6LL * sms && src.d / (chunks * 2) >= 16) chunks *= 2;
+  const int zchunk = (src.d + chunks - 1) / chunks;
+  k_sobel3d_tile<S, WRAP><<<dim3(tx, ty, (src.d + zchunk - 1) / zchunk), 256, 0, st>>>(
+      (const S*)src.ptr, (float*)dst.ptr, src.w, src.h, src.d, zchunk);
+  count_launch();
+  return check_launch("sobel_3d (staged)");
+}
+
 template <class S, bool WRAP> clk_status launch_sobel(const Image& dst, const Image& src, cudaStream_t st) {
   const dim3 block(SBX, SBY);
   const int tx = (src.w / 2 + SBX - 1) / SBX, ty = ((src.h + 1) / 2 + SBY - 1) / SBY;
@@ -261,6 +441,19 @@ clk_status fast_sobel(const Image& dst, const Image& src, const Policy& p, cudaS
     return CLK_UNSUPPORTED_DTYPE;
   if ((uintptr_t)dst.ptr % 8 != 0 || (uintptr_t)src.ptr % (2 * dtype_size(src.dt)) != 0) return CLK_UNSUPPORTED_DTYPE;
   const bool wrap = !p.sobel_narrow;
+  // staged tiles when rows are whole 16-byte vectors
+  const int ve = 16 / dtype_size(src.dt);
+  if ((uintptr_t)src.ptr % 16 == 0 && src.w % ve == 0) {
+    switch (src.dt) {
+      case CLK_U16:
+        return wrap ? launch_sobel_tile<uint16_t, true>(dst, src, st) : launch_sobel_tile<uint16_t, false>(dst, src, st);
+      case CLK_U8:
+        return wrap ? launch_sobel_tile<uint8_t, true>(dst, src, st) : launch_sobel_tile<uint8_t, false>(dst, src, st);
+      case CLK_I16: return launch_sobel_tile<int16_t, false>(dst, src, st);
+      case CLK_I8: return launch_sobel_tile<int8_t, false>(dst, src, st);
+      case CLK_F32: return launch_sobel_tile<float, false>(dst, src, st);
+    }
+  }
   switch (src.dt) {
     case CLK_U16: return wrap ? launch_sobel<uint16_t, true>(dst, src, st) : launch_sobel<uint16_t, false>(dst, src, st);
     case CLK_U8: return wrap ? launch_sobel<uint8_t, true>(dst, src, st) : launch_sobel<uint8_t, false>(dst, src, st);
