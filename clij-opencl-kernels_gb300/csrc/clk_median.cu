@@ -45,12 +45,15 @@ template <class T, bool ODD> clk_status launch(Shape sh, const Image& dst, const
     int chunks = 1;
     while ((int64_t)tx * ty * chunks < 8LL * sms && src.d / (chunks * 2) >= 16) chunks *= 2;
     int zchunk = (src.d + chunks - 1) / chunks;
-    zchunk += zchunk & 1;  // box: outputs come in z pairs
+    zchunk += zchunk & 1;  // outputs come in z pairs
     const dim3 grid(tx, ty, (src.d + zchunk - 1) / zchunk);
     if (sh == BOX27)
       k_median_box27<T, ODD><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);
-    else
+    else if constexpr (sizeof(T) == 4)  // float keys: the pair kernel's registers would leave one CTA per SM
       k_median_sphere33<T, ODD><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);
+    else
+      k_median_sphere33_pair<T, ODD><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d,
+                                                             zchunk);
   }
   count_launch();
   return check_launch("median (networks)");

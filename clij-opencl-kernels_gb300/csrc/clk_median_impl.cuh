@@ -252,6 +252,73 @@ __device__ __forceinline__ void sphere33_tile(const T* __restrict__ src, T* __re
   }
 }
 
+// median_sphere_3d r=2 in z pairs: outputs z and z+1 both use the sorted
+// blocks of planes z and z+1, so their merge (net_merge99_r1_16) is computed
+// once; each output then takes rank 15 of those 16, the sorted block of its
+// other plane and its six singles (net_sphere33_pair_final).  187 min/max per
+// output instead of 220.
+template <class T, bool ODD>
+__device__ __forceinline__ void sphere33_pair_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H,
+                                                   int D, int zchunk, int bx, int by, int bz) {
+  using V = typename Px<T>::V;
+  const int x = 2 * (bx * BX + (int)threadIdx.x % BX);
+  const int y = by * BY + (int)threadIdx.x / BX;
+  if (x >= W || y >= H) return;
+  const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+  auto pl = [&](int z) { return src + (int64_t)clampi(z, D - 1) * plane; };
+  auto centre = [&](int z) { return load_pair<T, ODD>(pl(z) + (int64_t)y * W, x, W); };
+  // the six singles of output z: x -+ 2 and y -+ 2 in plane z, z -+ 2
+  auto singles = [&](int z, V (&s)[6]) {
+    const T* pc = pl(z);
+    V a, b, c;
+    row_cols<T, ODD>(pc + (int64_t)y * W, x, W, a, b, c, &s[0], &s[1]);
+    s[2] = load_pair<T, ODD>(pc + (int64_t)clampi(y - 2, H - 1) * W, x, W);
+    s[3] = load_pair<T, ODD>(pc + (int64_t)clampi(y + 2, H - 1) * W, x, W);
+    s[4] = centre(z - 2);
+    s[5] = centre(z + 2);
+  };
+  auto final = [&](const V (&m)[16], const V (&b)[9], const V (&s)[6]) {
+    V w[31];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) w[k] = m[k];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) w[16 + k] = b[k];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w[25 + k] = s[k];
+    net_sphere33_pair_final_raw(w);
+    return w[net_sphere33_pair_final_out[0]];
+  };
+  V bm1[9], b0[9], b1[9], b2[9];  // sorted blocks of planes zo-1 .. zo+2
+  block9<T, ODD>(pl(z0 - 1), x, y, W, H, bm1);
+  block9<T, ODD>(pl(z0), x, y, W, H, b0);
+  block9<T, ODD>(pl(z0 + 1), x, y, W, H, b1);
+  block9<T, ODD>(pl(z0 + 2), x, y, W, H, b2);
+  for (int zo = z0; zo < z1; zo += 2) {
+    V m[16];
+    {
+      V w[18];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) w[k] = b0[k], w[9 + k] = b1[k];
+      net_merge99_r1_16_raw(w);
+      pick(w, net_merge99_r1_16_out, m);
+    }
+    V s[6];
+    singles(zo, s);
+    store_pair<T, ODD>(dst + (int64_t)zo * plane + (int64_t)y * W, x, W, final(m, bm1, s));
+    if (zo + 1 < z1) {
+      singles(zo + 1, s);
+      store_pair<T, ODD>(dst + (int64_t)(zo + 1) * plane + (int64_t)y * W, x, W, final(m, b2, s));
+    }
+    if (zo + 2 < z1) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) bm1[k] = b1[k], b0[k] = b2[k];
+      block9<T, ODD>(pl(zo + 3), x, y, W, H, b1);
+      block9<T, ODD>(pl(zo + 4), x, y, W, H, b2);
+    }
+  }
+}
+
 // median_box_2d 3x3.
 template <class T, bool ODD>
 __device__ __forceinline__ void box9_2d_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int bx,
@@ -283,6 +350,15 @@ __global__ void __launch_bounds__(BX * BY) k_median_box27(const T* __restrict__ 
 // four CTAs per SM instead of three
 template <class T> constexpr int sphere_min_ctas() { return sizeof(T) == 2 ? 4 : sizeof(T) == 1 ? 3 : 2; }
 
+// the z-pair kernel holds four sorted blocks and the shared merge
+template <class T> constexpr int sphere_pair_min_ctas() { return 2; }
+
+template <class T, bool ODD>
+__global__ void __launch_bounds__(BX * BY, sphere_pair_min_ctas<T>()) k_median_sphere33_pair(const T* __restrict__ src,
+                                                                                     T* __restrict__ dst, int W,
+                                                                                     int H, int D, int zchunk) {
+  sphere33_pair_tile<T, ODD>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
+}
 template <class T, bool ODD>
 __global__ void __launch_bounds__(BX * BY, sphere_min_ctas<T>()) k_median_sphere33(const T* __restrict__ src, T* __restrict__ dst, int W,
                                                              int H, int D, int zchunk) {

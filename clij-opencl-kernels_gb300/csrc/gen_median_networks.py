@@ -18,6 +18,8 @@ Networks (V is a SIMD word: two 16-bit lanes, one output each):
   net_merge99_mid      two sorted 9s -> ranks 4..13 of their merge
   net_box27_final      rank 9 of (ranks 4..13 of 18) U (sorted 9) = median of 27
   net_sphere33_final   rank 16 of (sorted 9 U sorted 9 U sorted 9 U 4 U 2) = median of 33
+  net_merge99_r1_16    two sorted 9s -> ranks 1..16 (the shared merge of a z pair)
+  net_sphere33_pair_final  rank 15 of (ranks 1..16 U sorted 9 U 6) = median of 33
   net_sort4 / net_sort2 helpers
 """
 from __future__ import annotations
@@ -169,6 +171,33 @@ def main():
            lambda v, o: o[allr[16]] == sorted(v)[16], exhaustive=False, trials=200000)
     stats["sphere33_final"] = ops(prog)
     parts.append(("net_sphere33_final_raw", 33, prog, [allr[16]], "sorted 9 x3 + 4 + 2 singles -> rank 16"))
+
+    # sphere33 in z pairs: outputs z and z+1 share the blocks of planes z and
+    # z+1.  Their merge drops rank 0 (below the median: 17 of the 18 are
+    # larger, so at most 15 of the other 15 values can be smaller) and rank
+    # 17 (above it), keeping ranks 1..16 ...
+    net = []
+    r = oe_merge(list(range(9)), list(range(9, 18)), net)
+    prog = prune(net, r[1:17])
+    verify(prog, 18, [list(range(9)), list(range(9, 18))],
+           lambda v, o: [o[w] for w in r[1:17]] == sorted(v)[1:17], exhaustive=True)
+    stats["merge99_r1_16"] = ops(prog)
+    parts.append(("net_merge99_r1_16_raw", 18, prog, r[1:17], "sorted 9s w[0..8], w[9..17] -> ranks 1..16"))
+
+    # ... and each output takes rank 15 of those 16 (w[0..15], sorted), the
+    # sorted block of its other plane (w[16..24]), its four in-plane
+    # singles (w[25..28]) and its two z singles (w[29], w[30]).
+    net = []
+    s4 = oe_merge(oe_merge([25], [26], net), oe_merge([27], [28], net), net)
+    s6 = oe_merge(s4, oe_merge([29], [30], net), net)
+    q = oe_merge(list(range(16, 25)), s6, net)
+    allr = oe_merge(list(range(16)), q, net)
+    prog = prune(net, [allr[15]])
+    verify(prog, 31, [list(range(16)), list(range(16, 25))],
+           lambda v, o: o[allr[15]] == sorted(v)[15], exhaustive=False, trials=200000)
+    stats["sphere33_pair_final"] = ops(prog)
+    parts.append(("net_sphere33_pair_final_raw", 31, prog, [allr[15]],
+                  "sorted 16 w[0..15] U sorted 9 w[16..24] U 6 singles -> rank 15"))
 
     # 2D: median of 9 from three sorted triples (median_box_2d 3x3)
     net = []

@@ -47,6 +47,26 @@ int main() {
     bad |= check<19>("box27_final", {{0,10},{10,19}}, net_box27_final_out, 1, 9, [](int (&w)[19]) { net_box27_final_raw(w); }, vm);
     bad |= check<33>("sphere33_final", {{0,9},{9,18},{18,27}}, net_sphere33_final_out, 1, 16, [](int (&w)[33]) { net_sphere33_final_raw(w); }, vm);
     bad |= check<9>("med9", {{0,3},{3,6},{6,9}}, net_med9_out, 1, 4, [](int (&w)[9]) { net_med9_raw(w); }, vm);
+    bad |= check<18>("merge99_r1_16", {{0,9},{9,18}}, net_merge99_r1_16_out, 16, 1, [](int (&w)[18]) { net_merge99_r1_16_raw(w); }, vm);
+    bad |= check<31>("sphere33_pair_final", {{0,16},{16,25}}, net_sphere33_pair_final_out, 1, 15,
+                     [](int (&w)[31]) { net_sphere33_pair_final_raw(w); }, vm);
+    // the z-pair composition: median of 33 = rank 15 of (ranks 1..16 of the
+    // shared planes' merge, the other plane's sorted 9, 6 singles)
+    for (int t = 0; t < 200000; ++t) {
+      std::vector<int> v(33);
+      for (auto& x : v) x = (int)(rng() % vm);
+      runs(v, {{0,9},{9,18},{18,27}});
+      std::vector<int> s = v;
+      std::sort(s.begin(), s.end());
+      int m[18];
+      for (int i = 0; i < 18; ++i) m[i] = v[i];
+      net_merge99_r1_16_raw(m);
+      int w[31];
+      for (int i = 0; i < 16; ++i) w[i] = m[net_merge99_r1_16_out[i]];
+      for (int i = 0; i < 15; ++i) w[16 + i] = v[18 + i];
+      net_sphere33_pair_final_raw(w);
+      if (w[net_sphere33_pair_final_out[0]] != s[16]) { std::puts("FAIL sphere33 pair composition"); bad = 1; break; }
+    }
   }
   std::puts(bad ? "FAILED" : "ok");
   return bad;
