@@ -362,6 +362,109 @@ def run_serve(args):
     print(json.dumps(line))
 
 
+def neighbours_spec():
+    """The filters either side of the path, on the suite's stack and mask:
+    (name, kernel, params, src, dst dtype code, bytes/voxel)."""
+    return [
+        ("minimum_sphere r1", "minimum_sphere_3d", {"Nx": 3, "Ny": 3, "Nz": 3}, "img", 2, 4),
+        ("maximum_sphere r1", "maximum_sphere_3d", {"Nx": 3, "Ny": 3, "Nz": 3}, "img", 2, 4),
+        ("mean_sphere r1", "mean_sphere_3d", {"Nx": 3, "Ny": 3, "Nz": 3}, "img", 2, 4),
+        ("minimum_sphere r2", "minimum_sphere_3d", {"Nx": 5, "Ny": 5, "Nz": 5}, "img", 2, 4),
+        ("mean_sphere r2", "mean_sphere_3d", {"Nx": 5, "Ny": 5, "Nz": 5}, "img", 2, 4),
+        ("minimum_slice_by_slice_sphere r2", "minimum_slice_by_slice_sphere_3d", {"Nx": 5, "Ny": 5}, "img", 2, 4),
+        ("median_slice_by_slice_box r1", "median_slice_by_slice_box_3d", {"Nx": 3, "Ny": 3}, "img", 2, 4),
+        ("erode_sphere_slice_by_slice", "erode_sphere_slice_by_slice_3d", {}, "mask", 0, 2),
+        ("greater_constant 400", "greater_constant_3d", {"scalar": 400.0}, "img", 0, 3),
+        ("copy u16->f32", "copy_3d", {}, "img", 4, 6),
+    ]
+
+
+def run_neighbours(args):
+    """The neighbourhood filters either side of the path, each its own
+    clk_execute call on the 1024x1024x256 u16 stack (u8 mask for the
+    morphology), with the reference kernels timed on a 256x256x32 sample."""
+    import torch
+
+    import clk
+    from clk import synth
+
+    torch.cuda.set_device(0)
+    peak, peak_kind = hbm_peak()
+    img = synth.blobs(SHAPE, N_BLOBS, seed=SEED, dtype=torch.uint16)
+    mask = synth.mask_of(img, 400.0)
+    V = img.numel()
+    spec = neighbours_spec()
+    if args.filters:
+        import re
+        spec = [t for t in spec if re.search(args.filters, t[0])]
+    srcs = {"img": img, "mask": mask}
+    outs = {t[0]: torch.empty(SHAPE, dtype=clk.torch_dtype(t[4]), device="cuda") for t in spec}
+    stream = torch.cuda.current_stream()
+
+    def call(t):
+        name, kernel, params, srcn, ddt, bpv = t
+        p = {("src1" if kernel.startswith("greater_constant") else "src"): srcs[srcn], "dst": outs[name]}
+        p.update(params)
+        clk.execute(kernel, p, stream=stream)
+
+    for _ in range(max(3, args.warmup)):
+        for t in spec:
+            call(t)
+    torch.cuda.synchronize()
+    ev = {t[0]: [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                 for _ in range(args.steps)] for t in spec}
+    t_begin, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = clk.launch_count()
+    with Clocks(0) as clocks:
+        torch.cuda.synchronize()
+        t_begin.record(stream)
+        for k in range(args.steps):
+            for t in spec:
+                ev[t[0]][k][0].record(stream)
+                call(t)
+                ev[t[0]][k][1].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    launches = clk.launch_count() - launches0
+    total_ms = t_begin.elapsed_time(t_end)
+    per = {}
+    for name, kernel, params, srcn, ddt, bpv in spec:
+        ms = statistics.mean(a.elapsed_time(b) for a, b in ev[name])
+        per[name] = {"ms": round(ms, 4), "gvox_s": round(V / (ms * 1e-3) / 1e9, 2),
+                     "hbm_frac": round(V * bpv / (ms * 1e-3) / 1e9 / peak, 4), "bytes_per_voxel": bpv}
+    cpu = None
+    if not args.no_cpu_baseline:
+        import numpy as np
+
+        from oracle import oracle as O
+        kind = "reference" if O.ref_available() else "port"
+        a = np.ascontiguousarray(img.cpu().numpy()[:SAMPLE[0], :SAMPLE[1], :SAMPLE[2]])
+        m = np.ascontiguousarray(mask.cpu().numpy()[:SAMPLE[0], :SAMPLE[1], :SAMPLE[2]])
+        nt = os.cpu_count() or 1
+        NP = {0: np.uint8, 2: np.uint16, 4: np.float32}
+        t0 = time.perf_counter()
+        for name, kernel, params, srcn, ddt, bpv in spec:
+            ints = [v for n, v in params.items() if n != "scalar"]
+            floats = [v for n, v in params.items() if n == "scalar"]
+            O.execute(kernel, a if srcn == "img" else m, NP[ddt], ints, floats,
+                      impl="ref" if kind == "reference" else "port", nthreads=nt)
+        dt = time.perf_counter() - t0
+        cpu = {"value": a.size * len(spec) / dt / 1e9, "unit": "Gvoxel/s", "cores": nt, "kind": kind,
+               "sample": f"{SAMPLE[2]}x{SAMPLE[1]}x{SAMPLE[0]} corner of the stack x {len(spec)} filters, {dt:.1f} s"}
+    line = {
+        "metric": "Gvoxel/s (neighbourhood filters either side of the path, 1024x1024x256)",
+        "value": round(V * len(spec) * args.steps / (total_ms * 1e-3) / 1e9, 3), "unit": "Gvoxel/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u16 in (u8 mask); u16/u8/f32 out", "data": "synthetic: the suite's seeded blob stack and mask",
+        "config": {"workload": "neighbourhood filters either side of the path on 1024x1024x256 uint16, each its "
+                               "own call", "voxels": V, "l2": "inputs larger than L2; no flush"},
+        "per_filter": per, "gpu_launches": launches, "clocks": clocks.result, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 LARGE_SHAPE = (400, 2048, 2048)  # (z, y, x): 6.71 GB of float32
 
 
@@ -477,10 +580,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--shape", default="", help="suite stack as z,y,x (default 256,1024,1024)")
     ap.add_argument("--filters", default="", help="regex selecting suite filters by name")
-    ap.add_argument("--workload", default="suite", choices=["suite", "batch", "serve", "large"],
+    ap.add_argument("--workload", default="suite", choices=["suite", "batch", "serve", "large", "neighbours"],
                     help="suite: plain filter suite on 1024x1024x256 u16 (default); batch: top-hat chain over 512 uneven "
                          "images; serve: Poisson-arrival requests; large: large-halo f32 "
-                         "filters on 2048x2048x400")
+                         "filters on 2048x2048x400; neighbours: the filters either side of the path")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -488,6 +591,8 @@ def main():
         return run_batch(args)
     if args.workload == "large":
         return run_large(args)
+    if args.workload == "neighbours":
+        return run_neighbours(args)
     if args.workload == "serve":
         return run_serve(args)
 

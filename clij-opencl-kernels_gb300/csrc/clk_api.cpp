@@ -78,13 +78,13 @@ void box_taps(int N, SepTaps* t) {
 // The median neighbourhood in the kernels' loop order (x, then y, then z;
 // median_sphere_3d_x.cl:55-72); the ellipsoid test in float as written
 // (:42-61), with FLT_MIN for a zero semi-axis.
-bool median_nbhd(bool sphere, int ndim, int Nx, int Ny, int Nz, MedianNbhd* m) {
+bool median_nbhd(bool sphere, int ndim, int Nx, int Ny, int Nz, MedianNbhd* m, bool guard) {
   const int ex = (Nx - 1) / 2, ey = (Ny - 1) / 2, ez = ndim == 3 ? (Nz - 1) / 2 : 0;
   if (ex > 127 || ey > 127 || ez > 127) return false;
   float a2 = (float)(ex * ex), b2 = (float)(ey * ey), c2 = (float)(ez * ez);
-  if (a2 == 0) a2 = 1.17549435e-38f;
-  if (b2 == 0) b2 = 1.17549435e-38f;
-  if (c2 == 0) c2 = 1.17549435e-38f;
+  if (guard && a2 == 0) a2 = 1.17549435e-38f;
+  if (guard && b2 == 0) b2 = 1.17549435e-38f;
+  if (guard && c2 == 0) c2 = 1.17549435e-38f;
   int n = 0;
   for (int x = -ex; x <= ex; ++x) {
     const float xs = (float)(x * x);
@@ -118,7 +118,13 @@ bool median_nbhd(bool sphere, int ndim, int Nx, int Ny, int Nz, MedianNbhd* m) {
 
 namespace {
 
-enum Family { F_SEP, F_MEDIAN, F_MORPH, F_SOBEL };
+enum Family { F_SEP, F_MEDIAN, F_MORPH, F_SOBEL, F_RANK, F_THRESH, F_COPY };
+// sub bits of the families that take a neighbourhood
+// (F_RANK keeps its operation in bits 0-1 and its value mode in bits 2-3)
+constexpr int kSphere = 1;      // F_MEDIAN
+constexpr int kPlanar = 16;     // F_MEDIAN / F_MORPH / F_RANK: 2-D neighbourhood on each plane of a 3-D image
+constexpr int kNoGuard = 32;    // F_MEDIAN: no FLT_MIN guard for a zero semi-axis
+constexpr int rank_sub(RankOp op, RankMode mode, bool planar) { return (int)op | ((int)mode << 2) | (planar ? kPlanar : 0); }
 
 struct ParamSpec {
   const char* name;
@@ -137,6 +143,7 @@ struct KernelInfo {
 constexpr ParamSpec kDst{"dst", CLK_ARG_IMAGE}, kSrc{"src", CLK_ARG_IMAGE};
 constexpr ParamSpec kDim{"dim", CLK_ARG_INT}, kN{"N", CLK_ARG_INT}, kS{"s", CLK_ARG_FLOAT};
 constexpr ParamSpec kNx{"Nx", CLK_ARG_INT}, kNy{"Ny", CLK_ARG_INT}, kNz{"Nz", CLK_ARG_INT};
+constexpr ParamSpec kSrc1{"src1", CLK_ARG_IMAGE}, kScalar{"scalar", CLK_ARG_FLOAT};
 
 // Parameter lists in the .cl declaration order.
 const KernelInfo kRegistry[] = {
@@ -162,6 +169,26 @@ const KernelInfo kRegistry[] = {
     {"dilate_sphere_3d", F_MORPH, 3, 1, {kSrc, kDst}, 2},
     {"sobel_2d", F_SOBEL, 2, 0, {kDst, kSrc}, 2},  // sobel_2d_x.cl:3-7
     {"sobel_3d", F_SOBEL, 3, 0, {kDst, kSrc}, 2},  // sobel_3d_x.cl:3-7
+    // the neighbourhood filters either side of the path
+    {"minimum_sphere_2d", F_RANK, 2, rank_sub(RANK_MIN, RANK_CAST, false), {kDst, kSrc, kNx, kNy}, 4},  // :3-9
+    {"minimum_sphere_3d", F_RANK, 3, rank_sub(RANK_MIN, RANK_FLOAT, false), {kDst, kSrc, kNx, kNy, kNz}, 5},
+    {"maximum_sphere_2d", F_RANK, 2, rank_sub(RANK_MAX, RANK_CONVERT, false), {kDst, kSrc, kNx, kNy}, 4},
+    {"maximum_sphere_3d", F_RANK, 3, rank_sub(RANK_MAX, RANK_FLOAT, false), {kDst, kSrc, kNx, kNy, kNz}, 5},
+    {"mean_sphere_2d", F_RANK, 2, rank_sub(RANK_MEAN, RANK_FLOAT, false), {kDst, kSrc, kNx, kNy}, 4},
+    {"mean_sphere_3d", F_RANK, 3, rank_sub(RANK_MEAN, RANK_FLOAT, false), {kDst, kSrc, kNx, kNy, kNz}, 5},
+    {"minimum_slice_by_slice_sphere_3d", F_RANK, 3, rank_sub(RANK_MIN, RANK_CONVERT, true), {kDst, kSrc, kNx, kNy}, 4},
+    {"maximum_slice_by_slice_sphere_3d", F_RANK, 3, rank_sub(RANK_MAX, RANK_CONVERT, true), {kDst, kSrc, kNx, kNy}, 4},
+    {"mean_slice_by_slice_sphere_3d", F_RANK, 3, rank_sub(RANK_MEAN, RANK_FLOAT, true), {kDst, kSrc, kNx, kNy}, 4},
+    {"median_slice_by_slice_box_3d", F_MEDIAN, 3, kPlanar, {kDst, kSrc, kNx, kNy}, 4},
+    {"median_slice_by_slice_sphere_3d", F_MEDIAN, 3, kSphere | kPlanar | kNoGuard, {kDst, kSrc, kNx, kNy}, 4},
+    {"erode_box_slice_by_slice_3d", F_MORPH, 3, 2 | kPlanar, {kSrc, kDst}, 2},
+    {"erode_sphere_slice_by_slice_3d", F_MORPH, 3, 3 | kPlanar, {kSrc, kDst}, 2},
+    {"dilate_box_slice_by_slice_3d", F_MORPH, 3, 0 | kPlanar, {kSrc, kDst}, 2},
+    {"dilate_sphere_slice_by_slice_3d", F_MORPH, 3, 1 | kPlanar, {kSrc, kDst}, 2},
+    {"greater_constant_2d", F_THRESH, 2, 0, {kSrc1, kScalar, kDst}, 3},  // greater_constant_2d_x.cl:3-7
+    {"greater_constant_3d", F_THRESH, 3, 0, {kSrc1, kScalar, kDst}, 3},
+    {"copy_2d", F_COPY, 2, 0, {kDst, kSrc}, 2},  // copy_2d_x.cl
+    {"copy_3d", F_COPY, 3, 0, {kDst, kSrc}, 2},  // copy_3d_x.cl:3-6
 };
 constexpr int kRegistrySize = sizeof(kRegistry) / sizeof(kRegistry[0]);
 
@@ -336,7 +363,8 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
   Policy pol;
   if ((st = parse_defines(defines, ndefines, &pol))) return st;
   Image src, dst;
-  if ((st = to_image(b.a[slot_of(*k, "src")]->image, k->ndim, "src", &src))) return st;
+  const int src_slot = slot_of(*k, "src") >= 0 ? slot_of(*k, "src") : slot_of(*k, "src1");
+  if ((st = to_image(b.a[src_slot]->image, k->ndim, "src", &src))) return st;
   if ((st = to_image(b.a[slot_of(*k, "dst")]->image, k->ndim, "dst", &dst))) return st;
   Range r{dst.w, dst.h, dst.d};
   if (global) {
@@ -363,10 +391,12 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
       return direct_sep_pass((SepOp)k->sub, dst, src, dim, taps, r, pol, s);
     }
     case F_MEDIAN: {
+      const bool planar = (k->sub & kPlanar) != 0;
+      const int nd = planar ? 2 : k->ndim;  // dimensions of the neighbourhood
       const int Nx = b.ival(slot_of(*k, "Nx")), Ny = b.ival(slot_of(*k, "Ny"));
-      const int Nz = k->ndim == 3 ? b.ival(slot_of(*k, "Nz")) : 1;
+      const int Nz = nd == 3 ? b.ival(slot_of(*k, "Nz")) : 1;
       static thread_local MedianNbhd m;
-      if (!median_nbhd(k->sub != 0, k->ndim, Nx, Ny, Nz, &m))
+      if (!median_nbhd((k->sub & kSphere) != 0, nd, Nx, Ny, Nz, &m, (k->sub & kNoGuard) == 0))
         return fail(CLK_BAD_ARG, "%s: neighbourhood %d x %d x %d exceeds %d elements or radius 127", k->name, Nx, Ny,
                     Nz, kMaxMedian);
       if (m.n == 0) return fail(CLK_BAD_ARG, "%s: empty neighbourhood (Nx=%d Ny=%d Nz=%d)", k->name, Nx, Ny, Nz);
@@ -380,23 +410,50 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
                         src.d == dst.d;
       // float windows holding both -0 and +0 (or NaN) may pick the other zero
       // on the network path; CLK_EXACT_ORDER keeps the insertion sort for them
-      if (full && !(pol.exact_order && src.dt == CLK_F32)) {
-        st = fast_median(k->sub != 0, dst, src, m, s);
+      if (full && !planar && !(pol.exact_order && src.dt == CLK_F32)) {
+        st = fast_median((k->sub & kSphere) != 0, dst, src, m, s);
         if (st != CLK_UNSUPPORTED_DTYPE) return st;
       }
       return direct_median(dst, src, m, r, s);
     }
     case F_MORPH: {
-      const bool erode = (k->sub & 2) != 0, sphere = (k->sub & 1) != 0;
+      const bool erode = (k->sub & 2) != 0, sphere = (k->sub & 1) != 0, planar = (k->sub & kPlanar) != 0;
       if (r.count() == 0) return CLK_OK;
       if ((st = device_ready())) return st;
       const bool full = r.x == dst.w && r.y == dst.h && r.z == dst.d && src.w == dst.w && src.h == dst.h &&
                         src.d == dst.d;
-      if (full) {
+      if (full && !planar) {
         st = fast_morph(erode, sphere, 1, dst, src, pol, s);
         if (st != CLK_UNSUPPORTED_DTYPE) return st;
       }
-      return direct_morph(erode, sphere, dst, src, r, pol, s);
+      return direct_morph(erode, sphere, dst, src, r, pol, s, planar);
+    }
+    case F_RANK: {
+      const RankOp op = (RankOp)(k->sub & 3);
+      const RankMode mode = (RankMode)((k->sub >> 2) & 3);
+      const bool planar = (k->sub & kPlanar) != 0;
+      const int nd = planar ? 2 : k->ndim;
+      const int Nx = b.ival(slot_of(*k, "Nx")), Ny = b.ival(slot_of(*k, "Ny"));
+      const int Nz = nd == 3 ? b.ival(slot_of(*k, "Nz")) : 1;
+      static thread_local MedianNbhd m;
+      if (!median_nbhd(true, nd, Nx, Ny, Nz, &m))
+        return fail(CLK_BAD_ARG, "%s: neighbourhood %d x %d x %d exceeds %d elements or radius 127", k->name, Nx, Ny,
+                    Nz, kMaxMedian);
+      if (r.count() == 0) return CLK_OK;
+      if ((st = device_ready())) return st;
+      return direct_rank(op, mode, dst, src, m, r, pol, s);
+    }
+    case F_THRESH:
+    case F_COPY: {
+      const bool greater = k->fam == F_THRESH;
+      const float scalar = greater ? b.fval(slot_of(*k, "scalar")) : 0.f;
+      if (r.count() == 0) return CLK_OK;
+      if ((st = device_ready())) return st;
+      if (r.x == dst.w && r.y == dst.h && r.z == dst.d) {
+        st = fast_pointwise(greater, dst, src, scalar, pol, s);
+        if (st != CLK_UNSUPPORTED_DTYPE) return st;
+      }
+      return greater ? direct_greater_constant(dst, src, scalar, r, s) : direct_copy(dst, src, r, pol, s);
     }
     case F_SOBEL: {
       if (r.count() == 0) return CLK_OK;
@@ -494,14 +551,14 @@ clk_status clk_morphology(const char* kernel_name, const clk_image* dst_img, con
     return fail(CLK_BAD_ARG, "%s: src and dst extents differ", k->name);
   if ((st = device_ready())) return st;
   cudaStream_t stm = (cudaStream_t)stream;
-  const bool erode = (k->sub & 2) != 0, sphere = (k->sub & 1) != 0;
+  const bool erode = (k->sub & 2) != 0, sphere = (k->sub & 1) != 0, planar = (k->sub & kPlanar) != 0;
   const Range r{dst.w, dst.h, dst.d};
   if (iterations == 0) return direct_copy(dst, src, r, pol, stm);
   // Each launch reads the previous result (dst-typed, like the orchestrator's
   // temporaries).  Pairs of iterations run fused where the pixel types and
   // layout allow; the chain of steps ping-pongs between a temporary and dst
   // so that the last step writes dst and no step reads what it writes.
-  const bool fuse = fast_morph_fusable(dst, src);
+  const bool fuse = !planar && fast_morph_fusable(dst, src);
   const int nsteps = fuse ? (iterations + 1) / 2 : iterations;
   void* tmp = nullptr;
   if (nsteps > 1) {
@@ -517,8 +574,8 @@ clk_status clk_morphology(const char* kernel_name, const clk_image* dst_img, con
     Image out = dst;
     if (i != nsteps - 1) out.ptr = ((nsteps - 1 - i) % 2 == 1) ? tmp : dst.ptr;
     const int take = (fuse && left >= 2) ? 2 : 1;
-    st = fast_morph(erode, sphere, take, out, cur, pol, stm);
-    if (st == CLK_UNSUPPORTED_DTYPE && take == 1) st = direct_morph(erode, sphere, out, cur, r, pol, stm);
+    st = planar ? CLK_UNSUPPORTED_DTYPE : fast_morph(erode, sphere, take, out, cur, pol, stm);
+    if (st == CLK_UNSUPPORTED_DTYPE && take == 1) st = direct_morph(erode, sphere, out, cur, r, pol, stm, planar);
     left -= take;
     cur = out;
   }
@@ -531,6 +588,7 @@ int clk_supported(const char* kernel_name, int32_t src_dtype, int32_t dst_dtype,
   if (!k || k->ndim != ndim) return 0;
   if (src_dtype < CLK_U8 || src_dtype > CLK_F32 || dst_dtype < CLK_U8 || dst_dtype > CLK_F32) return 0;
   if (k->fam == F_MEDIAN && src_dtype != dst_dtype) return 0;
+  if (k->fam == F_RANK && ((k->sub >> 2) & 3) == RANK_CAST && src_dtype == CLK_F32 && dst_dtype != CLK_F32) return 0;
   return 1;
 }
 

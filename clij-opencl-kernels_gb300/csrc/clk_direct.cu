@@ -4,6 +4,8 @@
 // FMA), so their results are bit-identical to the reference's.  They back
 // clk_execute's single-pass drop-in and every case the fused fast paths do
 // not cover.
+#include <type_traits>
+
 #include "clk_common.cuh"
 
 namespace clk {
@@ -94,6 +96,72 @@ __global__ void __launch_bounds__(kBlock)
       a[j + 1] = t;
     }
     dst[at(dd, x, y, z)] = a[n / 2];
+  }
+}
+
+// .x of a read: uint for unsigned pixels, int for signed, float for float
+template <class S> __device__ __forceinline__ auto readx(const S* p, int64_t i) {
+  const S t = __ldg(p + i);
+  if constexpr (std::is_same<S, float>::value) return t;
+  else if constexpr (std::is_signed<S>::value) return (int)t;
+  else return (unsigned)t;
+}
+
+// minimum/maximum/mean over the sphere offsets in loop order (x, y, z):
+// minimum/maximum_sphere_3d_x.cl:15-49 (RANK_FLOAT: float running value,
+// CONVERT at the end), maximum_sphere_2d_x.cl:16-45 and
+// minimum/maximum_slice_by_slice_sphere_3d_x.cl:15-38 (RANK_CONVERT: dst-typed
+// value, CONVERT of every read), minimum_sphere_2d_x.cl:16-47 (RANK_CAST: the
+// reads C-cast to the dst type), mean_sphere_{2d,3d}_x.cl and
+// mean_slice_by_slice_sphere_3d_x.cl (float sum in loop order,
+// CONVERT(sum / count)).
+template <class S, class D, int OP, int MODE>
+__global__ void __launch_bounds__(kBlock)
+    k_rank(D* __restrict__ dst, const S* __restrict__ src, Dims3 sd, Dims3 dd, Range r,
+           const __grid_constant__ MedianNbhd m, bool rte) {
+  const int n = m.n;
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    D res;
+    if constexpr (OP == RANK_MEAN) {
+      float sum = 0.f;
+      for (int k = 0; k < n; ++k) {
+        const char4 o = m.off[k];
+        sum = __fadd_rn(sum, (float)readx(src, atc(sd, x + o.x, y + o.y, z + o.z)));
+      }
+      res = convert_sat<D>(__fdiv_rn(sum, (float)n), rte);
+    } else if constexpr (MODE == RANK_FLOAT) {
+      float v = (float)readx(src, atc(sd, x, y, z));
+      for (int k = 0; k < n; ++k) {
+        const char4 o = m.off[k];
+        const float t = (float)readx(src, atc(sd, x + o.x, y + o.y, z + o.z));
+        if (OP == RANK_MIN ? t < v : t > v) v = t;
+      }
+      res = convert_sat<D>(v, rte);
+    } else {
+      D v = convert_sat<D>((float)readx(src, atc(sd, x, y, z)), rte);
+      for (int k = 0; k < n; ++k) {
+        const char4 o = m.off[k];
+        const auto rv = readx(src, atc(sd, x + o.x, y + o.y, z + o.z));
+        const D t = MODE == RANK_CAST ? (D)rv : convert_sat<D>((float)rv, rte);
+        if (OP == RANK_MIN ? t < v : t > v) v = t;
+      }
+      res = v;
+    }
+    dst[at(dd, x, y, z)] = res;
+  }
+}
+
+// greater_constant_{2d,3d}_x.cl:10-17
+template <class S, class D>
+__global__ void __launch_bounds__(kBlock)
+    k_greater_constant(D* __restrict__ dst, const S* __restrict__ src, Dims3 sd, Dims3 dd, Range r, float scalar) {
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    const float in = (float)readx(src, atc(sd, x, y, z));
+    dst[at(dd, x, y, z)] = in > scalar ? (D)1 : (D)0;
   }
 }
 
@@ -239,6 +307,45 @@ clk_status direct_copy(const Image& dst, const Image& src, Range r, const Policy
   return check_launch("copy");
 }
 
+clk_status direct_rank(RankOp op, RankMode mode, const Image& dst, const Image& src, const MedianNbhd& m, Range r,
+                       const Policy& p, cudaStream_t st) {
+  if (r.count() == 0) return CLK_OK;
+  if (mode == RANK_CAST && src.dt == CLK_F32 && dst.dt != CLK_F32)
+    return fail(CLK_UNSUPPORTED_DTYPE, "minimum_sphere_2d: float to integer (the kernel's C cast of an out-of-range "
+                                       "float is undefined)");
+  const unsigned g = grid_for(r.count());
+  const bool ok = dispatch_types(src.dt, dst.dt, [&](auto s, auto d) {
+    using S = decltype(s);
+    using D = decltype(d);
+    auto* o = (D*)dst.ptr;
+    auto* in = (const S*)src.ptr;
+    const Dims3 a = dims(src), b = dims(dst);
+    if (op == RANK_MEAN) k_rank<S, D, RANK_MEAN, RANK_FLOAT><<<g, kBlock, 0, st>>>(o, in, a, b, r, m, p.rte);
+    else if (op == RANK_MIN && mode == RANK_FLOAT) k_rank<S, D, RANK_MIN, RANK_FLOAT><<<g, kBlock, 0, st>>>(o, in, a, b, r, m, p.rte);
+    else if (op == RANK_MAX && mode == RANK_FLOAT) k_rank<S, D, RANK_MAX, RANK_FLOAT><<<g, kBlock, 0, st>>>(o, in, a, b, r, m, p.rte);
+    else if (op == RANK_MIN && mode == RANK_CONVERT) k_rank<S, D, RANK_MIN, RANK_CONVERT><<<g, kBlock, 0, st>>>(o, in, a, b, r, m, p.rte);
+    else if (op == RANK_MAX && mode == RANK_CONVERT) k_rank<S, D, RANK_MAX, RANK_CONVERT><<<g, kBlock, 0, st>>>(o, in, a, b, r, m, p.rte);
+    else if (op == RANK_MIN) k_rank<S, D, RANK_MIN, RANK_CAST><<<g, kBlock, 0, st>>>(o, in, a, b, r, m, p.rte);
+    else k_rank<S, D, RANK_MAX, RANK_CAST><<<g, kBlock, 0, st>>>(o, in, a, b, r, m, p.rte);
+  });
+  if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "rank filter: pixel types %d -> %d", src.dt, dst.dt);
+  count_launch();
+  return check_launch("rank filter");
+}
+
+clk_status direct_greater_constant(const Image& dst, const Image& src, float scalar, Range r, cudaStream_t st) {
+  if (r.count() == 0) return CLK_OK;
+  const unsigned g = grid_for(r.count());
+  const bool ok = dispatch_types(src.dt, dst.dt, [&](auto s, auto d) {
+    using S = decltype(s);
+    using D = decltype(d);
+    k_greater_constant<S, D><<<g, kBlock, 0, st>>>((D*)dst.ptr, (const S*)src.ptr, dims(src), dims(dst), r, scalar);
+  });
+  if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "greater_constant: pixel types %d -> %d", src.dt, dst.dt);
+  count_launch();
+  return check_launch("greater_constant");
+}
+
 clk_status direct_median(const Image& dst, const Image& src, const MedianNbhd& m, Range r, cudaStream_t st) {
   if (r.count() == 0) return CLK_OK;
   if (src.dt != dst.dt)
@@ -260,10 +367,10 @@ clk_status direct_median(const Image& dst, const Image& src, const MedianNbhd& m
 }
 
 clk_status direct_morph(bool erode, bool sphere, const Image& dst, const Image& src, Range r, const Policy& p,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool planar) {
   if (r.count() == 0) return CLK_OK;
   const unsigned g = grid_for(r.count());
-  const bool three = src.ndim == 3;
+  const bool three = src.ndim == 3 && !planar;  // slice-by-slice: the 2-D kernel on every plane
   const bool ok = dispatch_types(src.dt, dst.dt, [&](auto s, auto d) {
     using S = decltype(s);
     using D = decltype(d);

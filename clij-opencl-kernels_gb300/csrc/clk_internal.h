@@ -74,7 +74,11 @@ int* wait_flag_device();
 int dtype_size(int dt);
 bool gauss_taps(int N, float s, SepTaps* t);  // false: window too large
 void box_taps(int N, SepTaps* t);
-bool median_nbhd(bool sphere, int ndim, int Nx, int Ny, int Nz, MedianNbhd* m);
+// guard = false reproduces median_slice_by_slice_sphere_3d_x.cl:39-45, which
+// omits the FLT_MIN guard (a zero semi-axis leaves the neighbourhood empty)
+bool median_nbhd(bool sphere, int ndim, int Nx, int Ny, int Nz, MedianNbhd* m, bool guard = true);
+enum RankOp { RANK_MIN = 0, RANK_MAX = 1, RANK_MEAN = 2 };
+enum RankMode { RANK_FLOAT = 0, RANK_CONVERT = 1, RANK_CAST = 2 };
 
 // The validated inputs of a whole separable filter (the checks of
 // clk_separable): kernel, images, policy, per-axis taps and skipped axes.
@@ -95,8 +99,15 @@ clk_status direct_sep_pass(SepOp op, const Image& dst, const Image& src, int dim
                            const Policy& p, cudaStream_t st);
 clk_status direct_copy(const Image& dst, const Image& src, Range r, const Policy& p, cudaStream_t st);
 clk_status direct_median(const Image& dst, const Image& src, const MedianNbhd& m, Range r, cudaStream_t st);
+clk_status direct_rank(RankOp op, RankMode mode, const Image& dst, const Image& src, const MedianNbhd& m, Range r,
+                       const Policy& p, cudaStream_t st);
+clk_status direct_greater_constant(const Image& dst, const Image& src, float scalar, Range r, cudaStream_t st);
+// whole-image copy (greater = false) or greater_constant, vectorised
+// (clk_pointwise.cu); CLK_UNSUPPORTED_DTYPE where extents or alignment differ
+clk_status fast_pointwise(bool greater, const Image& dst, const Image& src, float scalar, const Policy& p,
+                          cudaStream_t st);
 clk_status direct_morph(bool erode, bool sphere, const Image& dst, const Image& src, Range r, const Policy& p,
-                        cudaStream_t st);
+                        cudaStream_t st, bool planar = false);
 clk_status direct_sobel(const Image& dst, const Image& src, Range r, const Policy& p, cudaStream_t st);
 
 // ---- fused / tiled fast paths.  Return CLK_UNSUPPORTED_DTYPE (without

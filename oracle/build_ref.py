@@ -48,6 +48,14 @@ KERNELS = [
     "erode_box_2d", "erode_box_3d", "erode_sphere_2d", "erode_sphere_3d",
     "dilate_box_2d", "dilate_box_3d", "dilate_sphere_2d", "dilate_sphere_3d",
     "sobel_2d", "sobel_3d",
+    # the neighbourhood filters either side of the path
+    "minimum_sphere_2d", "minimum_sphere_3d", "maximum_sphere_2d", "maximum_sphere_3d",
+    "mean_sphere_2d", "mean_sphere_3d",
+    "minimum_slice_by_slice_sphere_3d", "maximum_slice_by_slice_sphere_3d", "mean_slice_by_slice_sphere_3d",
+    "median_slice_by_slice_box_3d", "median_slice_by_slice_sphere_3d",
+    "erode_box_slice_by_slice_3d", "erode_sphere_slice_by_slice_3d",
+    "dilate_box_slice_by_slice_3d", "dilate_sphere_slice_by_slice_3d",
+    "greater_constant_2d", "greater_constant_3d", "copy_2d", "copy_3d",
 ]
 # pixel types in clk_dtype order (include/clk.h)
 DTYPES = [("u8", "uint8_t"), ("i8", "int8_t"), ("u16", "uint16_t"),
@@ -118,8 +126,8 @@ def generate(reference: Path = DEFAULT_REFERENCE) -> list[Path]:
                 ns = f"clkcl::{k}__{sn}_{dn}"
                 args, ni, nf = [], 0, 0
                 for kind, ident in params:
-                    if kind == "image":
-                        args.append(ident)
+                    if kind == "image":  # src / src1 -> the input, dst -> the output
+                        args.append("src" if ident.startswith("src") else ident)
                     elif kind == "int":
                         args.append(f"c->ia[{ni}]"); ni += 1
                     else:

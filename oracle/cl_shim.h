@@ -134,6 +134,10 @@ struct clk_sobel_array {
 #define IMAGE_src_PIXEL_TYPE SRC_T
 #define IMAGE_dst_PIXEL_TYPE DST_T
 #define READ_src_IMAGE(img, smp, ...) clk_read(img, __VA_ARGS__)
+// greater_constant_{2d,3d}_x.cl name their input src1
+#define IMAGE_src1_TYPE clk_img<SRC_T>
+#define IMAGE_src1_PIXEL_TYPE SRC_T
+#define READ_src1_IMAGE(img, smp, ...) clk_read(img, __VA_ARGS__)
 #define WRITE_dst_IMAGE(img, ...) clk_write(img, __VA_ARGS__)
 #define CONVERT_dst_PIXEL_TYPE(x) clk_convert_sat<DST_T>(x)
 #ifndef MAX_ARRAY_SIZE

@@ -28,6 +28,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -136,12 +137,14 @@ template <class S, class D> static void copy_conv(const Vol& dst, const Vol& src
 // Neighbourhood offsets of median_box/median_sphere in the kernels' loop
 // order (x outer, then y, then z; median_sphere_3d_x.cl:55-72), with the
 // sphere test evaluated in float exactly as written (:42-61).
-static std::vector<int> median_offsets(bool sphere, int ndim, int Nx, int Ny, int Nz) {
+// guard = false: median_slice_by_slice_sphere_3d_x.cl:39-45 has no FLT_MIN
+// guard, so a zero semi-axis gives 0/0 and an empty neighbourhood.
+static std::vector<int> median_offsets(bool sphere, int ndim, int Nx, int Ny, int Nz, bool guard = true) {
   const int ex = (Nx - 1) / 2, ey = (Ny - 1) / 2, ez = ndim == 3 ? (Nz - 1) / 2 : 0;
   float a2 = (float)(ex * ex), b2 = (float)(ey * ey), c2 = (float)(ez * ez);
-  if (a2 == 0) a2 = FLT_MIN;
-  if (b2 == 0) b2 = FLT_MIN;
-  if (c2 == 0) c2 = FLT_MIN;
+  if (guard && a2 == 0) a2 = FLT_MIN;
+  if (guard && b2 == 0) b2 = FLT_MIN;
+  if (guard && c2 == 0) c2 = FLT_MIN;
   std::vector<int> off;
   for (int x = -ex; x <= ex; ++x) {
     const float xs = (float)(x * x);
@@ -188,6 +191,10 @@ static void median(const Vol& dst, const Vol& src, const std::vector<int>& off, 
 // erode_sphere_3d_x.cl:14-37, dilate_box_3d_x.cl:14-37,
 // dilate_sphere_3d_x.cl:14-38), replaying the early-exit loops so that the
 // zero that is finally written (its sign, for float images) is the same one.
+// The slice-by-slice variants (erode_box_slice_by_slice_3d_x.cl:14-31,
+// erode_sphere_slice_by_slice_3d_x.cl:14-26, dilate_box_slice_by_slice_3d_x.cl,
+// dilate_sphere_slice_by_slice_3d_x.cl) are the 2-D kernels on every plane of a
+// 3-D image: ndim = 2 semantics with z unchanged.
 template <class S, class D>
 static void morph(bool erode, bool sphere, int ndim, const Vol& dst, const Vol& src, const int g[3], int flags,
                   int nt) {
@@ -302,6 +309,82 @@ static void sobel3d(const Vol& dst, const Vol& src, const int g[3], int flags, i
   }
 }
 
+// minimum/maximum/mean_sphere_{2d,3d} and the slice-by-slice sphere
+// variants: a reduction over the ellipsoid (ellipse) offsets in the kernels'
+// loop order (x outer, then y, then z).  The variants differ in the type the
+// running value lives in:
+//   RANK_FLOAT    float, values (float)READ(..).x, result CONVERT(value)
+//                 (minimum/maximum_sphere_3d_x.cl:15-49);
+//   RANK_CONVERT  dst type, centre and values CONVERT(READ(..).x), result
+//                 the value (maximum_sphere_2d_x.cl:16-45,
+//                 minimum/maximum_slice_by_slice_sphere_3d_x.cl:15-38);
+//   RANK_CAST     dst type, centre CONVERT, values the C cast
+//                 (IMAGE_dst_PIXEL_TYPE)READ(..).x (minimum_sphere_2d_x.cl:16-47);
+// and the mean sums READ(..).x into a float in loop order and writes
+// CONVERT(sum / count) (mean_sphere_3d_x.cl:16-56, mean_sphere_2d_x.cl,
+// mean_slice_by_slice_sphere_3d_x.cl:16-41).
+enum RankOp { RANK_MIN, RANK_MAX, RANK_MEAN };
+enum RankMode { RANK_FLOAT, RANK_CONVERT, RANK_CAST };
+
+template <class S> static inline auto readx(const Vol& v, int x, int y, int z) {
+  // .x of a read: uint for unsigned, int for signed, float for float
+  const S t = ((const S*)v.p)[vidx(v, x, y, z)];
+  if constexpr (std::is_same<S, float>::value) return t;
+  else if constexpr (std::is_signed<S>::value) return (int)t;
+  else return (unsigned)t;
+}
+
+template <class S, class D>
+static void rank_filter(RankOp op, RankMode mode, const Vol& dst, const Vol& src, const std::vector<int>& off,
+                        const int g[3], int flags, int nt) {
+  const int n = (int)off.size() / 3;
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (long zy = 0; zy < (long)g[2] * g[1]; ++zy) {
+    const int z = (int)(zy / g[1]), y = (int)(zy % g[1]);
+    for (int x = 0; x < g[0]; ++x) {
+      D res;
+      if (op == RANK_MEAN) {
+        float sum = 0;
+        int count = 0;
+        for (int i = 0; i < n; ++i) {
+          sum = sum + (float)readx<S>(src, x + off[3 * i], y + off[3 * i + 1], z + off[3 * i + 2]);
+          count++;
+        }
+        res = convert_sat<D>((double)(sum / (float)count), flags);
+      } else if (mode == RANK_FLOAT) {
+        float m = (float)readx<S>(src, x, y, z);
+        for (int i = 0; i < n; ++i) {
+          const float v = (float)readx<S>(src, x + off[3 * i], y + off[3 * i + 1], z + off[3 * i + 2]);
+          if (op == RANK_MIN ? v < m : v > m) m = v;
+        }
+        res = convert_sat<D>((double)m, flags);
+      } else {
+        D m = convert_sat<D>((double)readx<S>(src, x, y, z), flags);
+        for (int i = 0; i < n; ++i) {
+          const auto r = readx<S>(src, x + off[3 * i], y + off[3 * i + 1], z + off[3 * i + 2]);
+          const D v = mode == RANK_CAST ? (D)r : convert_sat<D>((double)r, flags);
+          if (op == RANK_MIN ? v < m : v > m) m = v;
+        }
+        res = m;
+      }
+      ((D*)dst.p)[(long)x + (long)dst.w * ((long)y + (long)dst.h * z)] = res;
+    }
+  }
+}
+
+// greater_constant_{2d,3d}_x.cl:10-17: (float)READ(src1).x > scalar ? 1 : 0.
+template <class S, class D>
+static void greater_constant(const Vol& dst, const Vol& src, float scalar, const int g[3], int nt) {
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (long zy = 0; zy < (long)g[2] * g[1]; ++zy) {
+    const int z = (int)(zy / g[1]), y = (int)(zy % g[1]);
+    for (int x = 0; x < g[0]; ++x) {
+      const float in = (float)readx<S>(src, x, y, z);
+      ((D*)dst.p)[(long)x + (long)dst.w * ((long)y + (long)dst.h * z)] = in > scalar ? (D)1 : (D)0;
+    }
+  }
+}
+
 // ---------------------------------------------------------------- dispatch
 template <class F> static int with_types(int sdt, int ddt, F f) {
   auto d = [&](auto s) -> int {
@@ -359,10 +442,37 @@ int clko_execute(const char* kernel, int sdt, int ddt, const void* src, const in
       return 0;
     });
   }
+  // slice-by-slice kernels: a 2-D neighbourhood on every plane of a 3-D image
+  const bool planar = k.find("slice_by_slice") != std::string::npos;
+  const int nbdim = planar ? 2 : ndim;
+  if (starts(k, "minimum_sphere_") || starts(k, "maximum_sphere_") || starts(k, "mean_sphere_") ||
+      starts(k, "minimum_slice_by_slice_sphere") || starts(k, "maximum_slice_by_slice_sphere") ||
+      starts(k, "mean_slice_by_slice_sphere")) {
+    const RankOp op = starts(k, "minimum") ? RANK_MIN : starts(k, "maximum") ? RANK_MAX : RANK_MEAN;
+    const RankMode mode = (ndim == 3 && !planar) ? RANK_FLOAT : (k == "minimum_sphere_2d" ? RANK_CAST : RANK_CONVERT);
+    if (mode == RANK_CAST && sdt == F32 && ddt != F32) return -2;  // C cast of an out-of-range float: undefined
+    const auto off = median_offsets(true, nbdim, ia[0], ia[1], nbdim == 3 ? ia[2] : 1);
+    return with_types(sdt, ddt, [&](auto s, auto d) {
+      rank_filter<decltype(s), decltype(d)>(op, mode, D, S, off, g, flags, nt);
+      return 0;
+    });
+  }
+  if (starts(k, "greater_constant_"))
+    return with_types(sdt, ddt, [&](auto s, auto d) {
+      greater_constant<decltype(s), decltype(d)>(D, S, fa[0], g, nt);
+      return 0;
+    });
+  if (k == "copy_2d" || k == "copy_3d")
+    return with_types(sdt, ddt, [&](auto s, auto d) {
+      copy_conv<decltype(s), decltype(d)>(D, S, flags, nt);
+      return 0;
+    });
   if (starts(k, "median_")) {
     if (sdt != ddt) return -2;
-    const bool sphere = starts(k, "median_sphere");
-    const auto off = median_offsets(sphere, ndim, ia[0], ia[1], ndim == 3 ? ia[2] : 1);
+    const bool sphere = k.find("sphere") != std::string::npos;
+    const auto off = median_offsets(sphere, nbdim, ia[0], ia[1], nbdim == 3 ? ia[2] : 1,
+                                    k != "median_slice_by_slice_sphere_3d");
+    if (off.empty()) return -3;  // the kernel would read an uninitialised array element
     return with_types(sdt, ddt, [&](auto s, auto d) {
       median<decltype(s), decltype(d)>(D, S, off, g, nt);
       return 0;
@@ -372,7 +482,7 @@ int clko_execute(const char* kernel, int sdt, int ddt, const void* src, const in
     const bool erode = starts(k, "erode_");
     const bool sphere = k.find("sphere") != std::string::npos;
     return with_types(sdt, ddt, [&](auto s, auto d) {
-      morph<decltype(s), decltype(d)>(erode, sphere, ndim, D, S, g, flags, nt);
+      morph<decltype(s), decltype(d)>(erode, sphere, nbdim, D, S, g, flags, nt);
       return 0;
     });
   }

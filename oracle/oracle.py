@@ -38,6 +38,13 @@ KERNELS = [
     "erode_box_2d", "erode_box_3d", "erode_sphere_2d", "erode_sphere_3d",
     "dilate_box_2d", "dilate_box_3d", "dilate_sphere_2d", "dilate_sphere_3d",
     "sobel_2d", "sobel_3d",
+    "minimum_sphere_2d", "minimum_sphere_3d", "maximum_sphere_2d", "maximum_sphere_3d",
+    "mean_sphere_2d", "mean_sphere_3d",
+    "minimum_slice_by_slice_sphere_3d", "maximum_slice_by_slice_sphere_3d", "mean_slice_by_slice_sphere_3d",
+    "median_slice_by_slice_box_3d", "median_slice_by_slice_sphere_3d",
+    "erode_box_slice_by_slice_3d", "erode_sphere_slice_by_slice_3d",
+    "dilate_box_slice_by_slice_3d", "dilate_sphere_slice_by_slice_3d",
+    "greater_constant_2d", "greater_constant_3d", "copy_2d", "copy_3d",
 ]
 
 

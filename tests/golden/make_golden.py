@@ -59,7 +59,19 @@ def main() -> None:
     for k in O.KERNELS:
         is2 = k.endswith("2d")
         shapes = [(10, 13), (1, 6)] if is2 else [(5, 7, 9), (1, 3, 8)]
-        if k.startswith(("gaussian", "mean", "minimum", "maximum")):
+        if "slice_by_slice" in k and not k.startswith(("erode", "dilate")):
+            pairs = PAIRS_MEDIAN if k.startswith("median") else PAIRS_SEP
+            cases = [{"Nx": 3, "Ny": 3}, {"Nx": 5, "Ny": 5}, {"Nx": 5, "Ny": 3}]
+        elif "_sphere_" in k and k.startswith(("minimum", "maximum", "mean")):
+            pairs = [p for p in PAIRS_SEP if not (k == "minimum_sphere_2d" and p[0] == "f32" and p[1] != "f32")]
+            cases = ([{"Nx": 3, "Ny": 3}, {"Nx": 5, "Ny": 5}, {"Nx": 5, "Ny": 3}] if is2 else
+                     [{"Nx": 3, "Ny": 3, "Nz": 3}, {"Nx": 5, "Ny": 5, "Nz": 5}, {"Nx": 3, "Ny": 5, "Nz": 1}])
+        elif k.startswith("greater_constant"):
+            pairs = PAIRS_SEP
+            cases = [{"scalar": 400.0}, {"scalar": -2.5}]
+        elif k.startswith("copy"):
+            pairs, cases = PAIRS_SEP, [{}]
+        elif k.startswith(("gaussian", "mean", "minimum", "maximum")):
             pairs = PAIRS_SEP
             cases = [{"dim": d, "N": N, "s": s} for d in ((0, 1) if is2 else (0, 1, 2))
                      for N, s in ((5, 1.0), (8, 2.5))]
@@ -75,8 +87,8 @@ def main() -> None:
             for sdt, ddt in pairs:
                 a = image(rng, shp, sdt, binary=k.startswith(("erode", "dilate")))
                 for c in cases:
-                    ints = [v for n, v in c.items() if n != "s"]
-                    floats = [c["s"]] if "s" in c else []
+                    ints = [v for n, v in c.items() if n not in ("s", "scalar")]
+                    floats = [v for n, v in c.items() if n in ("s", "scalar")]
                     out = O.execute(k, a, NP[ddt], ints, floats, impl="ref")
                     add("execute", k, sdt, ddt, c, a, out)
     for k in ("gaussian_blur_separable_3d", "mean_separable_3d", "minimum_separable_3d", "maximum_separable_3d",

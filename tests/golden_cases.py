@@ -15,7 +15,10 @@ def load():
         yield c, z[c["key"] + "_in"], z[c["key"] + "_out"]
 
 
+FLOAT_PARAMS = ("s", "scalar")
+
+
 def split_params(params):
-    ints = [v for n, v in params.items() if n != "s"]
-    floats = [params["s"]] if "s" in params else []
+    ints = [v for n, v in params.items() if n not in FLOAT_PARAMS]
+    floats = [v for n, v in params.items() if n in FLOAT_PARAMS]
     return ints, floats

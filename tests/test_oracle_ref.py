@@ -19,6 +19,13 @@ def _kernels():
 
 def _cases(k):
     is2 = k.endswith("2d")
+    if "slice_by_slice" in k and not k.startswith(("erode", "dilate")):
+        return [((3, 3), ()), ((5, 5), ()), ((5, 3), ()), ((1, 7), ())]
+    if "_sphere_" in k and k.startswith(("minimum", "maximum", "mean")):
+        return [((3, 3), ()), ((5, 5), ()), ((5, 3), ()), ((1, 7), ())] if is2 else \
+            [((3, 3, 3), ()), ((5, 5, 5), ()), ((3, 5, 1), ()), ((7, 3, 5), ()), ((1, 1, 9), ())]
+    if k.startswith("greater_constant"):
+        return [((), (400.0,)), ((), (-3.5,)), ((), (0.0,))]
     if k.startswith(("gaussian", "mean", "minimum", "maximum")):
         dims = (0, 1) if is2 else (0, 1, 2)
         return [((d, N), (s,)) for d in dims for N, s in ((5, 1.5), (7, 2.0), (4, 0.7), (1, 1.0), (0, 1.0),
@@ -48,8 +55,12 @@ def test_port_matches_reference(oracle, kernel):
             for ddt in DTYPES:
                 if kernel.startswith("median") and sdt != ddt:
                     continue
+                if kernel == "minimum_sphere_2d" and sdt == np.float32 and ddt != np.float32:
+                    continue  # C cast of an out-of-range float: undefined in the kernel
                 a = random_image(rng, shp, sdt, binary=morph)
                 for ia, fa in _cases(kernel):
+                    if kernel == "median_slice_by_slice_sphere_3d" and min(ia) <= 2:
+                        continue  # no FLT_MIN guard there: empty neighbourhood (rejected by the library)
                     r = O.execute(kernel, a, ddt, ia, fa, impl="ref")
                     p = O.execute(kernel, a, ddt, ia, fa, impl="port")
                     assert r.tobytes() == p.tobytes(), (kernel, shp, np.dtype(sdt), np.dtype(ddt), ia, fa)
