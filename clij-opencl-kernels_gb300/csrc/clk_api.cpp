@@ -410,7 +410,7 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
                         src.d == dst.d;
       // float windows holding both -0 and +0 (or NaN) may pick the other zero
       // on the network path; CLK_EXACT_ORDER keeps the insertion sort for them
-      if (full && !planar && !(pol.exact_order && src.dt == CLK_F32)) {
+      if (full && !(pol.exact_order && src.dt == CLK_F32)) {
         st = fast_median((k->sub & kSphere) != 0, dst, src, m, s);
         if (st != CLK_UNSUPPORTED_DTYPE) return st;
       }
@@ -441,6 +441,12 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
                     Nz, kMaxMedian);
       if (r.count() == 0) return CLK_OK;
       if ((st = device_ready())) return st;
+      const bool full = r.x == dst.w && r.y == dst.h && r.z == dst.d && src.w == dst.w && src.h == dst.h &&
+                        src.d == dst.d;
+      if (full) {
+        st = fast_sphere_rank(op, planar, dst, src, m, s);
+        if (st != CLK_UNSUPPORTED_DTYPE) return st;
+      }
       return direct_rank(op, mode, dst, src, m, r, pol, s);
     }
     case F_THRESH:

@@ -102,6 +102,10 @@ clk_status direct_median(const Image& dst, const Image& src, const MedianNbhd& m
 clk_status direct_rank(RankOp op, RankMode mode, const Image& dst, const Image& src, const MedianNbhd& m, Range r,
                        const Policy& p, cudaStream_t st);
 clk_status direct_greater_constant(const Image& dst, const Image& src, float scalar, Range r, cudaStream_t st);
+// min / max / mean over the radius-1 and radius-2 spheres (disks when planar
+// or 2-D) for 8/16-bit pixels, src type = dst type (clk_sphere_rank.cu)
+clk_status fast_sphere_rank(RankOp op, bool planar, const Image& dst, const Image& src, const MedianNbhd& m,
+                            cudaStream_t st);
 // whole-image copy (greater = false) or greater_constant, vectorised
 // (clk_pointwise.cu); CLK_UNSUPPORTED_DTYPE where extents or alignment differ
 clk_status fast_pointwise(bool greater, const Image& dst, const Image& src, float scalar, const Policy& p,

@@ -29,7 +29,9 @@ enum Shape { BOX27, SPHERE33, BOX9_2D, OTHER };
 Shape classify(bool sphere, const MedianNbhd& m, int ndim) {
   if (ndim == 3 && !sphere && m.ex == 1 && m.ey == 1 && m.ez == 1 && m.n == 27) return BOX27;
   if (ndim == 3 && sphere && m.ex == 2 && m.ey == 2 && m.ez == 2 && m.n == 33) return SPHERE33;
-  if (ndim == 2 && m.ex == 1 && m.ey == 1 && m.n == 9) return BOX9_2D;  // box, or the 3x3 "sphere" that is a box
+  // 3x3 in every plane: the 2-D box (or the 3x3 "sphere" that is a box), a
+  // 3-D box with Nz = 1, the slice-by-slice box
+  if (m.ex == 1 && m.ey == 1 && m.ez == 0 && m.n == 9) return BOX9_2D;
   return OTHER;
 }
 
@@ -37,7 +39,7 @@ template <class T, bool ODD> clk_status launch(Shape sh, const Image& dst, const
   const dim3 block(BX * BY);
   const int tx = ((src.w + 1) / 2 + BX - 1) / BX, ty = (src.h + BY - 1) / BY;
   if (sh == BOX9_2D) {
-    k_median_box9_2d<T, ODD><<<dim3(tx, ty), block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h);
+    k_median_box9_2d<T, ODD><<<dim3(tx, ty, src.d), block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h);
   } else {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);

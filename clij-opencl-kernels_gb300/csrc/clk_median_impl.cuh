@@ -367,7 +367,10 @@ __global__ void __launch_bounds__(BX * BY, sphere_min_ctas<T>()) k_median_sphere
 template <class T, bool ODD>
 __global__ void __launch_bounds__(BX * BY) k_median_box9_2d(const T* __restrict__ src, T* __restrict__ dst, int W,
                                                             int H) {
-  box9_2d_tile<T, ODD>(src, dst, W, H, blockIdx.x, blockIdx.y);
+  // one plane per blockIdx.z: a 2-D image, or a 3x3 neighbourhood on every
+  // plane of a 3-D image (Nz = 1, slice by slice)
+  const int64_t plane = (int64_t)W * H * blockIdx.z;
+  box9_2d_tile<T, ODD>(src + plane, dst + plane, W, H, blockIdx.x, blockIdx.y);
 }
 
 }  // namespace med
