@@ -374,6 +374,9 @@ def neighbours_spec():
         ("minimum_slice_by_slice_sphere r2", "minimum_slice_by_slice_sphere_3d", {"Nx": 5, "Ny": 5}, "img", 2, 4),
         ("median_slice_by_slice_box r1", "median_slice_by_slice_box_3d", {"Nx": 3, "Ny": 3}, "img", 2, 4),
         ("erode_sphere_slice_by_slice", "erode_sphere_slice_by_slice_3d", {}, "mask", 0, 2),
+        ("gradient_z", "gradient_z_3d", {}, "img", 4, 6),
+        ("laplace_diamond", "laplace_diamond_3d", {}, "img", 4, 6),
+        ("laplace_box", "laplace_box_3d", {}, "img", 4, 6),
         ("greater_constant 400", "greater_constant_3d", {"scalar": 400.0}, "img", 0, 3),
         ("copy u16->f32", "copy_3d", {}, "img", 4, 6),
     ]

@@ -118,7 +118,7 @@ bool median_nbhd(bool sphere, int ndim, int Nx, int Ny, int Nz, MedianNbhd* m, b
 
 namespace {
 
-enum Family { F_SEP, F_MEDIAN, F_MORPH, F_SOBEL, F_RANK, F_THRESH, F_COPY };
+enum Family { F_SEP, F_MEDIAN, F_MORPH, F_SOBEL, F_RANK, F_THRESH, F_COPY, F_STENCIL };
 // sub bits of the families that take a neighbourhood
 // (F_RANK keeps its operation in bits 0-1 and its value mode in bits 2-3)
 constexpr int kSphere = 1;      // F_MEDIAN
@@ -189,6 +189,15 @@ const KernelInfo kRegistry[] = {
     {"greater_constant_3d", F_THRESH, 3, 0, {kSrc1, kScalar, kDst}, 3},
     {"copy_2d", F_COPY, 2, 0, {kDst, kSrc}, 2},  // copy_2d_x.cl
     {"copy_3d", F_COPY, 3, 0, {kDst, kSrc}, 2},  // copy_3d_x.cl:3-6
+    {"gradient_x_2d", F_STENCIL, 2, ST_GRADIENT_X, {kDst, kSrc}, 2},  // gradient_x_2d_x.cl:1-5
+    {"gradient_y_2d", F_STENCIL, 2, ST_GRADIENT_Y, {kDst, kSrc}, 2},
+    {"gradient_x_3d", F_STENCIL, 3, ST_GRADIENT_X, {kDst, kSrc}, 2},
+    {"gradient_y_3d", F_STENCIL, 3, ST_GRADIENT_Y, {kDst, kSrc}, 2},
+    {"gradient_z_3d", F_STENCIL, 3, ST_GRADIENT_Z, {kDst, kSrc}, 2},
+    {"laplace_box_2d", F_STENCIL, 2, ST_LAPLACE_BOX_2D, {kDst, kSrc}, 2},  // laplace_box_2d_x.cl:3-7
+    {"laplace_box_3d", F_STENCIL, 3, ST_LAPLACE_BOX_3D, {kDst, kSrc}, 2},
+    {"laplace_diamond_2d", F_STENCIL, 2, ST_LAPLACE_DIAMOND_2D, {kDst, kSrc}, 2},
+    {"laplace_diamond_3d", F_STENCIL, 3, ST_LAPLACE_DIAMOND_3D, {kDst, kSrc}, 2},
 };
 constexpr int kRegistrySize = sizeof(kRegistry) / sizeof(kRegistry[0]);
 
@@ -422,8 +431,8 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
       if ((st = device_ready())) return st;
       const bool full = r.x == dst.w && r.y == dst.h && r.z == dst.d && src.w == dst.w && src.h == dst.h &&
                         src.d == dst.d;
-      if (full && !planar) {
-        st = fast_morph(erode, sphere, 1, dst, src, pol, s);
+      if (full) {
+        st = fast_morph(erode, sphere, 1, dst, src, pol, s, planar);
         if (st != CLK_UNSUPPORTED_DTYPE) return st;
       }
       return direct_morph(erode, sphere, dst, src, r, pol, s, planar);
@@ -448,6 +457,11 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
         if (st != CLK_UNSUPPORTED_DTYPE) return st;
       }
       return direct_rank(op, mode, dst, src, m, r, pol, s);
+    }
+    case F_STENCIL: {
+      if (r.count() == 0) return CLK_OK;
+      if ((st = device_ready())) return st;
+      return direct_stencil((StencilKind)k->sub, dst, src, r, pol, s);
     }
     case F_THRESH:
     case F_COPY: {
@@ -580,7 +594,7 @@ clk_status clk_morphology(const char* kernel_name, const clk_image* dst_img, con
     Image out = dst;
     if (i != nsteps - 1) out.ptr = ((nsteps - 1 - i) % 2 == 1) ? tmp : dst.ptr;
     const int take = (fuse && left >= 2) ? 2 : 1;
-    st = planar ? CLK_UNSUPPORTED_DTYPE : fast_morph(erode, sphere, take, out, cur, pol, stm);
+    st = fast_morph(erode, sphere, take, out, cur, pol, stm, planar);
     if (st == CLK_UNSUPPORTED_DTYPE && take == 1) st = direct_morph(erode, sphere, out, cur, r, pol, stm, planar);
     left -= take;
     cur = out;

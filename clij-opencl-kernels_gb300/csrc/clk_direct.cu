@@ -153,6 +153,64 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// gradient_{x,y,z}_{2d,3d}_x.cl: CONVERT(READ(+1).x - READ(-1).x) in float.
+template <class S, class D, int AXIS>
+__global__ void __launch_bounds__(kBlock)
+    k_gradient(D* __restrict__ dst, const S* __restrict__ src, Dims3 sd, Dims3 dd, Range r, bool rte) {
+  constexpr int dx = AXIS == 0, dy = AXIS == 1, dz = AXIS == 2;
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    const float a = (float)readx(src, atc(sd, x - dx, y - dy, z - dz));
+    const float b = (float)readx(src, atc(sd, x + dx, y + dy, z + dz));
+    dst[at(dd, x, y, z)] = convert_sat<D>(__fsub_rn(b, a), rte);
+  }
+}
+
+// laplace_diamond_{2d,3d}_x.cl, laplace_box_2d_x.cl: centre * K + each
+// neighbour * -1.0 in the expression's order, in double (the literals are
+// double), stored to float, converted.  KIND: 0 diamond 2-D, 1 diamond 3-D,
+// 2 box 2-D.
+template <class S, class D, int KIND>
+__global__ void __launch_bounds__(kBlock)
+    k_laplace_expr(D* __restrict__ dst, const S* __restrict__ src, Dims3 sd, Dims3 dd, Range r, bool rte) {
+  constexpr int NB = KIND == 0 ? 4 : KIND == 1 ? 6 : 8;
+  constexpr double K = KIND == 0 ? 4.0 : KIND == 1 ? 6.0 : 8.0;
+  // right, left, top, bottom, then front, back (3-D) or the corners A..D
+  constexpr signed char ox[8] = {1, -1, 0, 0, KIND == 1 ? 0 : -1, KIND == 1 ? 0 : 1, -1, 1};
+  constexpr signed char oy[8] = {0, 0, -1, 1, KIND == 1 ? 0 : -1, KIND == 1 ? 0 : -1, 1, 1};
+  constexpr signed char oz[8] = {0, 0, 0, 0, KIND == 1 ? 1 : 0, KIND == 1 ? -1 : 0, 0, 0};
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    double acc = __dmul_rn((double)(float)readx(src, atc(sd, x, y, z)), K);
+#pragma unroll
+    for (int k = 0; k < NB; ++k)
+      acc = __dadd_rn(acc, __dmul_rn((double)(float)readx(src, atc(sd, x + ox[k], y + oy[k], z + oz[k])), -1.0));
+    dst[at(dd, x, y, z)] = convert_sat<D>(__double2float_rn(acc), rte);
+  }
+}
+
+// laplace_box_3d_x.cl:13-25: float result over ax, ay, az; the centre adds
+// READ(..).x, the other taps READ(..).x * -1, which wraps for the uint reads
+// of unsigned pixels (2^32 - v).
+template <class S, class D>
+__global__ void __launch_bounds__(kBlock)
+    k_laplace_box3d(D* __restrict__ dst, const S* __restrict__ src, Dims3 sd, Dims3 dd, Range r, bool rte) {
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    float result = 0.f;
+    for (int ax = -1; ax <= 1; ++ax)
+      for (int ay = -1; ay <= 1; ++ay)
+        for (int az = -1; az <= 1; ++az) {
+          const auto v = readx(src, atc(sd, x + ax, y + ay, z + az));
+          result = __fadd_rn(result, (ax == 0 && ay == 0 && az == 0) ? (float)v : (float)(v * -1));
+        }
+    dst[at(dd, x, y, z)] = convert_sat<D>(result, rte);
+  }
+}
+
 // greater_constant_{2d,3d}_x.cl:10-17
 template <class S, class D>
 __global__ void __launch_bounds__(kBlock)
@@ -331,6 +389,31 @@ clk_status direct_rank(RankOp op, RankMode mode, const Image& dst, const Image& 
   if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "rank filter: pixel types %d -> %d", src.dt, dst.dt);
   count_launch();
   return check_launch("rank filter");
+}
+
+clk_status direct_stencil(StencilKind kind, const Image& dst, const Image& src, Range r, const Policy& p,
+                          cudaStream_t st) {
+  if (r.count() == 0) return CLK_OK;
+  const unsigned g = grid_for(r.count());
+  const bool ok = dispatch_types(src.dt, dst.dt, [&](auto s, auto d) {
+    using S = decltype(s);
+    using D = decltype(d);
+    auto* o = (D*)dst.ptr;
+    auto* in = (const S*)src.ptr;
+    const Dims3 a = dims(src), b = dims(dst);
+    switch (kind) {
+      case ST_GRADIENT_X: k_gradient<S, D, 0><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case ST_GRADIENT_Y: k_gradient<S, D, 1><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case ST_GRADIENT_Z: k_gradient<S, D, 2><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case ST_LAPLACE_DIAMOND_2D: k_laplace_expr<S, D, 0><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case ST_LAPLACE_DIAMOND_3D: k_laplace_expr<S, D, 1><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case ST_LAPLACE_BOX_2D: k_laplace_expr<S, D, 2><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+      case ST_LAPLACE_BOX_3D: k_laplace_box3d<S, D><<<g, kBlock, 0, st>>>(o, in, a, b, r, p.rte); break;
+    }
+  });
+  if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "stencil: pixel types %d -> %d", src.dt, dst.dt);
+  count_launch();
+  return check_launch("stencil");
 }
 
 clk_status direct_greater_constant(const Image& dst, const Image& src, float scalar, Range r, cudaStream_t st) {

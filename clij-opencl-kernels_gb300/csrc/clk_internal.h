@@ -102,6 +102,12 @@ clk_status direct_median(const Image& dst, const Image& src, const MedianNbhd& m
 clk_status direct_rank(RankOp op, RankMode mode, const Image& dst, const Image& src, const MedianNbhd& m, Range r,
                        const Policy& p, cudaStream_t st);
 clk_status direct_greater_constant(const Image& dst, const Image& src, float scalar, Range r, cudaStream_t st);
+enum StencilKind {
+  ST_GRADIENT_X, ST_GRADIENT_Y, ST_GRADIENT_Z,
+  ST_LAPLACE_DIAMOND_2D, ST_LAPLACE_DIAMOND_3D, ST_LAPLACE_BOX_2D, ST_LAPLACE_BOX_3D
+};
+clk_status direct_stencil(StencilKind kind, const Image& dst, const Image& src, Range r, const Policy& p,
+                          cudaStream_t st);
 // min / max / mean over the radius-1 and radius-2 spheres (disks when planar
 // or 2-D) for 8/16-bit pixels, src type = dst type (clk_sphere_rank.cu)
 clk_status fast_sphere_rank(RankOp op, bool planar, const Image& dst, const Image& src, const MedianNbhd& m,
@@ -138,7 +144,7 @@ clk_status sep_pass(SepOp op, const Image& dst, const Image& src, int axis, cons
 clk_status fused_separable(SepOp op, const Image& dst, const Image& src, const SepTaps taps[3], const bool skip[3],
                            const Policy& p, cudaStream_t st);
 clk_status fast_morph(bool erode, bool sphere, int iterations, const Image& dst, const Image& src, const Policy& p,
-                      cudaStream_t st);
+                      cudaStream_t st, bool planar = false);
 bool fast_morph_fusable(const Image& dst, const Image& src);  // fast_morph takes iterations = 2
 clk_status fast_sobel(const Image& dst, const Image& src, const Policy& p, cudaStream_t st);
 clk_status fast_median(bool sphere, const Image& dst, const Image& src, const MedianNbhd& m, cudaStream_t st);

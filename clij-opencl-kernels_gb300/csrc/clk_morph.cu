@@ -90,10 +90,13 @@ template <int ITER> struct Geo {
   static constexpr int SX = MX + 2, SY = MY + 2;      // staged intermediate planes
 };
 
+// ITER = 0: one step of the 2-D kernel on every plane of a 3-D image (the
+// slice-by-slice kernels, erode_sphere_slice_by_slice_3d_x.cl:14-26 ...).
 template <class S, class D, bool ERODE, bool SPHERE, int ITER>
 __global__ void __launch_bounds__(MT)
     k_morph_bytes(const S* __restrict__ src, D* __restrict__ dst, int W, int H, int Dz, int zchunk) {
   using G = Geo<ITER>;
+  constexpr bool PLANAR = ITER == 0;
   __shared__ uint4 in[3][G::IY * G::IX];
   __shared__ uint4 mid[ITER == 2 ? 3 : 1][ITER == 2 ? G::SY * G::SX : 1];
   const int nxc = W / 16;
@@ -103,14 +106,14 @@ __global__ void __launch_bounds__(MT)
   const int64_t plane = (int64_t)W * H;
   const uint4* src4 = reinterpret_cast<const uint4*>(src);
   uint4* dst4 = reinterpret_cast<uint4*>(dst);
-  const int hx = ITER, hy = ITER;  // halo of the staged input around the output tile
+  const int hx = PLANAR ? 1 : ITER, hy = hx;  // halo of the staged input around the output tile
 
   // Input planes are staged strictly in z order.  The next one is always in
   // flight in registers (pf) while the current planes are processed;
   // load_plane(zv, slot) stores plane zv (the prefetched one) as masks and
   // starts fetching zv + 1 if it will be needed.
   constexpr int NS = G::IY * G::IX, PERM = (NS + MT - 1) / MT;
-  const int last_in = z1 - 1 + ITER;
+  const int last_in = PLANAR ? z1 - 1 : z1 - 1 + ITER;
   uint4 pf[PERM];
   auto fetch = [&](int zv) {
     const int zc = clampi(zv, Dz - 1);
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(MT)
     }
     if (zv + 1 <= last_in) fetch(zv + 1);
   };
-  fetch(z0 - ITER);
+  fetch(PLANAR ? z0 : z0 - ITER);
   auto store = [&](int zo, int r, int q, uint4 m) {
     const int gy = y0 + r, gq = xc0 + q;
     if (gy < H && gq < nxc) {
@@ -141,7 +144,17 @@ __global__ void __launch_bounds__(MT)
     }
   };
 
-  if constexpr (ITER == 1) {
+  if constexpr (PLANAR) {
+    // each plane alone, two buffers: one barrier per plane
+    for (int zo = z0; zo < z1; ++zo) {
+      const int b = (zo - z0) & 1;
+      load_plane(zo, b);
+      __syncthreads();
+      const int r = tid / MX, q = tid % MX;
+      const int gq = xc0 + q;
+      store(zo, r, q, step<ERODE, SPHERE>(in[b], in[b], in[b], G::IX, r, q, gq == 0, gq == nxc - 1));
+    }
+  } else if constexpr (ITER == 1) {
     load_plane(z0 - 1, 0);
     load_plane(z0, 1);
     for (int zo = z0; zo < z1; ++zo) {
@@ -262,8 +275,13 @@ bool fast_morph_fusable(const Image& dst, const Image& src) {
 }
 
 clk_status fast_morph(bool erode, bool sphere, int iterations, const Image& dst, const Image& src, const Policy&,
-                      cudaStream_t st) {
+                      cudaStream_t st, bool planar) {
   if (!fast_morph_fusable(dst, src) || iterations < 1 || iterations > 2) return CLK_UNSUPPORTED_DTYPE;
+  if (planar) {
+    if (iterations != 1) return CLK_UNSUPPORTED_DTYPE;
+    if (erode) return sphere ? launch_sel<true, true, 0>(dst, src, st) : launch_sel<true, false, 0>(dst, src, st);
+    return sphere ? launch_sel<false, true, 0>(dst, src, st) : launch_sel<false, false, 0>(dst, src, st);
+  }
   const int sel = (erode ? 4 : 0) | (sphere ? 2 : 0) | (iterations == 2 ? 1 : 0);
   switch (sel) {
     case 0: return launch_sel<false, false, 1>(dst, src, st);

@@ -56,6 +56,8 @@ KERNELS = [
     "erode_box_slice_by_slice_3d", "erode_sphere_slice_by_slice_3d",
     "dilate_box_slice_by_slice_3d", "dilate_sphere_slice_by_slice_3d",
     "greater_constant_2d", "greater_constant_3d", "copy_2d", "copy_3d",
+    "gradient_x_2d", "gradient_y_2d", "gradient_x_3d", "gradient_y_3d", "gradient_z_3d",
+    "laplace_box_2d", "laplace_box_3d", "laplace_diamond_2d", "laplace_diamond_3d",
 ]
 # pixel types in clk_dtype order (include/clk.h)
 DTYPES = [("u8", "uint8_t"), ("i8", "int8_t"), ("u16", "uint16_t"),

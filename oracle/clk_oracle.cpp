@@ -385,6 +385,64 @@ static void greater_constant(const Vol& dst, const Vol& src, float scalar, const
   }
 }
 
+// gradient_{x,y,z}_{2d,3d}_x.cl: CONVERT(READ(+1).x - READ(-1).x), float
+// values and a float difference, along the kernel's axis.
+template <class S, class D>
+static void gradient(int axis, const Vol& dst, const Vol& src, const int g[3], int flags, int nt) {
+  const int dx = axis == 0, dy = axis == 1, dz = axis == 2;
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (long zy = 0; zy < (long)g[2] * g[1]; ++zy) {
+    const int z = (int)(zy / g[1]), y = (int)(zy % g[1]);
+    for (int x = 0; x < g[0]; ++x) {
+      const float a = (float)readx<S>(src, x - dx, y - dy, z - dz);
+      const float b = (float)readx<S>(src, x + dx, y + dy, z + dz);
+      ((D*)dst.p)[(long)x + (long)dst.w * ((long)y + (long)dst.h * z)] = convert_sat<D>((double)(b - a), flags);
+    }
+  }
+}
+
+// laplace_diamond_{2d,3d}_x.cl and laplace_box_2d_x.cl: float values, then
+// centre * K + each neighbour * -1.0 in the expression's order; the
+// literals are double, so the sum is evaluated in double and stored to float.
+template <class S, class D>
+static void laplace_expr(const std::vector<int>& nb, double k, const Vol& dst, const Vol& src, const int g[3],
+                         int flags, int nt) {
+  const int n = (int)nb.size() / 3;
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (long zy = 0; zy < (long)g[2] * g[1]; ++zy) {
+    const int z = (int)(zy / g[1]), y = (int)(zy % g[1]);
+    for (int x = 0; x < g[0]; ++x) {
+      double r = (double)(float)readx<S>(src, x, y, z) * k;
+      for (int i = 0; i < n; ++i)
+        r = r + (double)(float)readx<S>(src, x + nb[3 * i], y + nb[3 * i + 1], z + nb[3 * i + 2]) * -1.0;
+      const float res = (float)r;
+      ((D*)dst.p)[(long)x + (long)dst.w * ((long)y + (long)dst.h * z)] = convert_sat<D>((double)res, flags);
+    }
+  }
+}
+
+// laplace_box_3d_x.cl:13-25: float result, loop ax, ay, az; the centre adds
+// READ(..).x, every other tap READ(..).x * -1 -- an int times the read's .x,
+// which for unsigned pixels is a uint product that wraps (2^32 - v).
+template <class S, class D>
+static void laplace_box3d(const Vol& dst, const Vol& src, const int g[3], int flags, int nt) {
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (long zy = 0; zy < (long)g[2] * g[1]; ++zy) {
+    const int z = (int)(zy / g[1]), y = (int)(zy % g[1]);
+    for (int x = 0; x < g[0]; ++x) {
+      float result = 0;
+      for (int ax = -1; ax <= 1; ++ax)
+        for (int ay = -1; ay <= 1; ++ay)
+          for (int az = -1; az <= 1; ++az) {
+            const auto v = readx<S>(src, x + ax, y + ay, z + az);
+            if (ax == 0 && ay == 0 && az == 0) result = result + v;
+            else result = result + v * -1;
+          }
+      ((D*)dst.p)[(long)x + (long)dst.w * ((long)y + (long)dst.h * z)] = convert_sat<D>((double)result, flags);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- dispatch
 template <class F> static int with_types(int sdt, int ddt, F f) {
   auto d = [&](auto s) -> int {
@@ -454,6 +512,34 @@ int clko_execute(const char* kernel, int sdt, int ddt, const void* src, const in
     const auto off = median_offsets(true, nbdim, ia[0], ia[1], nbdim == 3 ? ia[2] : 1);
     return with_types(sdt, ddt, [&](auto s, auto d) {
       rank_filter<decltype(s), decltype(d)>(op, mode, D, S, off, g, flags, nt);
+      return 0;
+    });
+  }
+  if (starts(k, "gradient_")) {
+    const int axis = k[9] - 'x';
+    return with_types(sdt, ddt, [&](auto s, auto d) {
+      gradient<decltype(s), decltype(d)>(axis, D, S, g, flags, nt);
+      return 0;
+    });
+  }
+  if (k == "laplace_box_3d")
+    return with_types(sdt, ddt, [&](auto s, auto d) {
+      laplace_box3d<decltype(s), decltype(d)>(D, S, g, flags, nt);
+      return 0;
+    });
+  if (starts(k, "laplace_")) {
+    // neighbours in the expression's order: right, left, top, bottom(, front, back | A, B, C, D)
+    std::vector<int> nb = {1, 0, 0, -1, 0, 0, 0, -1, 0, 0, 1, 0};
+    double kc = 4.0;
+    if (k == "laplace_diamond_3d") {
+      nb.insert(nb.end(), {0, 0, 1, 0, 0, -1});
+      kc = 6.0;
+    } else if (k == "laplace_box_2d") {
+      nb.insert(nb.end(), {-1, -1, 0, 1, -1, 0, -1, 1, 0, 1, 1, 0});
+      kc = 8.0;
+    }
+    return with_types(sdt, ddt, [&](auto s, auto d) {
+      laplace_expr<decltype(s), decltype(d)>(nb, kc, D, S, g, flags, nt);
       return 0;
     });
   }

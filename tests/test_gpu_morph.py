@@ -9,7 +9,9 @@ from conftest import random_image
 
 pytestmark = pytest.mark.gpu
 
-MORPH = ["erode_sphere_3d", "dilate_sphere_3d", "erode_box_3d", "dilate_box_3d"]
+MORPH = ["erode_sphere_3d", "dilate_sphere_3d", "erode_box_3d", "dilate_box_3d",
+         "erode_sphere_slice_by_slice_3d", "dilate_sphere_slice_by_slice_3d",
+         "erode_box_slice_by_slice_3d", "dilate_box_slice_by_slice_3d"]
 
 
 @pytest.fixture(scope="module")
