@@ -9,3 +9,5 @@ from .api import Batch, Server, op_kernel, op_morphology, op_separable  # noqa: 
 from .api import (dilate_box, dilate_sphere, erode_box, erode_sphere, execute, gaussian_blur,  # noqa: F401
                   kernel_names, launch_count, morphology, maximum_box, mean_box, median_box, median_sphere, minimum_box,
                   separable, sigma_to_n, sobel, supported, torch_dtype, version, dtype_code, image_of)
+from .api import (convolve, copy, gradient, greater_constant, laplace, maximum_sphere, mean_sphere,  # noqa: F401
+                  minimum_sphere)

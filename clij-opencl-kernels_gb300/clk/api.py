@@ -230,6 +230,60 @@ def sobel(src, dst=None, stream=None, defines=None):
     return dst
 
 
+def _sphere(kind, src, dst, rx, ry, rz, stream, defines):
+    dst = _out(src, dst)
+    p = {"dst": dst, "src": src, "Nx": 2 * int(rx) + 1, "Ny": 2 * int(ry) + 1}
+    if src.dim() == 3:
+        p["Nz"] = 2 * int(rz) + 1
+    execute(kind + _suffix(src), p, defines=defines, stream=stream)
+    return dst
+
+
+def minimum_sphere(src, dst=None, radius_x=1, radius_y=1, radius_z=1, stream=None, defines=None):
+    return _sphere("minimum_sphere", src, dst, radius_x, radius_y, radius_z, stream, defines)
+
+
+def maximum_sphere(src, dst=None, radius_x=1, radius_y=1, radius_z=1, stream=None, defines=None):
+    return _sphere("maximum_sphere", src, dst, radius_x, radius_y, radius_z, stream, defines)
+
+
+def mean_sphere(src, dst=None, radius_x=1, radius_y=1, radius_z=1, stream=None, defines=None):
+    return _sphere("mean_sphere", src, dst, radius_x, radius_y, radius_z, stream, defines)
+
+
+def greater_constant(src, dst=None, scalar=0.0, stream=None, defines=None):
+    dst = _out(src, dst, torch.uint8)
+    execute("greater_constant" + _suffix(src), {"src1": src, "scalar": float(scalar), "dst": dst},
+            defines=defines, stream=stream)
+    return dst
+
+
+def copy(src, dst=None, stream=None, defines=None):
+    dst = _out(src, dst)
+    execute("copy" + _suffix(src), {"dst": dst, "src": src}, defines=defines, stream=stream)
+    return dst
+
+
+def gradient(src, dst=None, axis="x", stream=None, defines=None):
+    dst = _out(src, dst, torch.float32)
+    execute(f"gradient_{axis}" + _suffix(src), {"dst": dst, "src": src}, defines=defines, stream=stream)
+    return dst
+
+
+def laplace(src, dst=None, kind="box", stream=None, defines=None):
+    dst = _out(src, dst, torch.float32)
+    execute(f"laplace_{kind}" + _suffix(src), {"dst": dst, "src": src}, defines=defines, stream=stream)
+    return dst
+
+
+def convolve(src, kernel, dst=None, stream=None, defines=None):
+    """src * a float kernel image (convolve_3d_x.cl)."""
+    dst = _out(src, dst, torch.float32)
+    execute("convolve" + _suffix(src), {"src": src, "kernelImage": kernel.float().contiguous(), "dst": dst},
+            defines=defines, stream=stream)
+    return dst
+
+
 # ----------------------------------------------------------------- batch
 
 def op_separable(kernel: str, N, s=(0.0, 0.0, 0.0)) -> dict:

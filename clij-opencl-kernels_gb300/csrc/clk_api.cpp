@@ -118,7 +118,7 @@ bool median_nbhd(bool sphere, int ndim, int Nx, int Ny, int Nz, MedianNbhd* m, b
 
 namespace {
 
-enum Family { F_SEP, F_MEDIAN, F_MORPH, F_SOBEL, F_RANK, F_THRESH, F_COPY, F_STENCIL };
+enum Family { F_SEP, F_MEDIAN, F_MORPH, F_SOBEL, F_RANK, F_THRESH, F_COPY, F_STENCIL, F_CONV };
 // sub bits of the families that take a neighbourhood
 // (F_RANK keeps its operation in bits 0-1 and its value mode in bits 2-3)
 constexpr int kSphere = 1;      // F_MEDIAN
@@ -144,6 +144,7 @@ constexpr ParamSpec kDst{"dst", CLK_ARG_IMAGE}, kSrc{"src", CLK_ARG_IMAGE};
 constexpr ParamSpec kDim{"dim", CLK_ARG_INT}, kN{"N", CLK_ARG_INT}, kS{"s", CLK_ARG_FLOAT};
 constexpr ParamSpec kNx{"Nx", CLK_ARG_INT}, kNy{"Ny", CLK_ARG_INT}, kNz{"Nz", CLK_ARG_INT};
 constexpr ParamSpec kSrc1{"src1", CLK_ARG_IMAGE}, kScalar{"scalar", CLK_ARG_FLOAT};
+constexpr ParamSpec kKernelImage{"kernelImage", CLK_ARG_IMAGE};
 
 // Parameter lists in the .cl declaration order.
 const KernelInfo kRegistry[] = {
@@ -198,6 +199,8 @@ const KernelInfo kRegistry[] = {
     {"laplace_box_3d", F_STENCIL, 3, ST_LAPLACE_BOX_3D, {kDst, kSrc}, 2},
     {"laplace_diamond_2d", F_STENCIL, 2, ST_LAPLACE_DIAMOND_2D, {kDst, kSrc}, 2},
     {"laplace_diamond_3d", F_STENCIL, 3, ST_LAPLACE_DIAMOND_3D, {kDst, kSrc}, 2},
+    {"convolve_2d", F_CONV, 2, 0, {kSrc, kKernelImage, kDst}, 3},  // convolve_2d_x.cl:1-5
+    {"convolve_3d", F_CONV, 3, 0, {kSrc, kKernelImage, kDst}, 3},  // convolve_3d_x.cl:1-5
 };
 constexpr int kRegistrySize = sizeof(kRegistry) / sizeof(kRegistry[0]);
 
@@ -458,9 +461,22 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
       }
       return direct_rank(op, mode, dst, src, m, r, pol, s);
     }
+    case F_CONV: {
+      Image kern;
+      if ((st = to_image(b.a[slot_of(*k, "kernelImage")]->image, k->ndim, "kernelImage", &kern))) return st;
+      if (kern.dt != CLK_F32) return fail(CLK_UNSUPPORTED_DTYPE, "%s: the kernel image must be float", k->name);
+      if (r.count() == 0) return CLK_OK;
+      if ((st = device_ready())) return st;
+      return direct_convolve(dst, src, kern, r, pol, s);
+    }
     case F_STENCIL: {
       if (r.count() == 0) return CLK_OK;
       if ((st = device_ready())) return st;
+      const bool full = r.x == dst.w && r.y == dst.h && r.z == dst.d;
+      if (full && k->sub <= ST_GRADIENT_Z) {
+        st = fast_gradient(k->sub - ST_GRADIENT_X, dst, src, pol, s);
+        if (st != CLK_UNSUPPORTED_DTYPE) return st;
+      }
       return direct_stencil((StencilKind)k->sub, dst, src, r, pol, s);
     }
     case F_THRESH:

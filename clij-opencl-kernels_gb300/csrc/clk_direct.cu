@@ -183,11 +183,22 @@ __global__ void __launch_bounds__(kBlock)
   for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
     int x, y, z;
     decode(i, r, x, y, z);
-    double acc = __dmul_rn((double)(float)readx(src, atc(sd, x, y, z)), K);
+    float res;
+    if constexpr (std::is_integral<S>::value) {
+      // integer pixels: every partial sum is an integer far below 2^53, so the
+      // double evaluation is exact and equals this int32 sum
+      int acc = (int)readx(src, atc(sd, x, y, z)) * (int)K;
 #pragma unroll
-    for (int k = 0; k < NB; ++k)
-      acc = __dadd_rn(acc, __dmul_rn((double)(float)readx(src, atc(sd, x + ox[k], y + oy[k], z + oz[k])), -1.0));
-    dst[at(dd, x, y, z)] = convert_sat<D>(__double2float_rn(acc), rte);
+      for (int k = 0; k < NB; ++k) acc -= (int)readx(src, atc(sd, x + ox[k], y + oy[k], z + oz[k]));
+      res = (float)acc;
+    } else {
+      double acc = __dmul_rn((double)(float)readx(src, atc(sd, x, y, z)), K);
+#pragma unroll
+      for (int k = 0; k < NB; ++k)
+        acc = __dadd_rn(acc, __dmul_rn((double)(float)readx(src, atc(sd, x + ox[k], y + oy[k], z + oz[k])), -1.0));
+      res = __double2float_rn(acc);
+    }
+    dst[at(dd, x, y, z)] = convert_sat<D>(res, rte);
   }
 }
 
@@ -208,6 +219,28 @@ __global__ void __launch_bounds__(kBlock)
           result = __fadd_rn(result, (ax == 0 && ay == 0 && az == 0) ? (float)v : (float)(v * -1));
         }
     dst[at(dd, x, y, z)] = convert_sat<D>(result, rte);
+  }
+}
+
+// convolve_{2d,3d}_x.cl:17-31: c = kernel extent / 2; x, y, z over -c..c:
+// sum = sum + kernel(c + offset) * src(coord + offset), float multiply then
+// float add (no contraction), both reads clamped; CONVERT(sum).
+template <class S, class D>
+__global__ void __launch_bounds__(kBlock)
+    k_convolve(D* __restrict__ dst, const S* __restrict__ src, const float* __restrict__ kern, Dims3 sd, Dims3 kd,
+               Dims3 dd, Range r, bool rte) {
+  const int cx = kd.w / 2, cy = kd.h / 2, cz = kd.d / 2;
+  for (int64_t i = blockIdx.x * (int64_t)kBlock + threadIdx.x; i < r.count(); i += (int64_t)gridDim.x * kBlock) {
+    int x, y, z;
+    decode(i, r, x, y, z);
+    float sum = 0.f;
+    for (int a = -cx; a <= cx; ++a)
+      for (int b = -cy; b <= cy; ++b)
+        for (int c = -cz; c <= cz; ++c) {
+          const float kv = __ldg(kern + atc(kd, cx + a, cy + b, cz + c));
+          sum = __fadd_rn(sum, __fmul_rn(kv, (float)readx(src, atc(sd, x + a, y + b, z + c))));
+        }
+    dst[at(dd, x, y, z)] = convert_sat<D>(sum, rte);
   }
 }
 
@@ -414,6 +447,22 @@ clk_status direct_stencil(StencilKind kind, const Image& dst, const Image& src, 
   if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "stencil: pixel types %d -> %d", src.dt, dst.dt);
   count_launch();
   return check_launch("stencil");
+}
+
+clk_status direct_convolve(const Image& dst, const Image& src, const Image& kern, Range r, const Policy& p,
+                           cudaStream_t st) {
+  if (r.count() == 0) return CLK_OK;
+  if (kern.dt != CLK_F32) return fail(CLK_UNSUPPORTED_DTYPE, "convolve: the kernel image must be float");
+  const unsigned g = grid_for(r.count());
+  const bool ok = dispatch_types(src.dt, dst.dt, [&](auto s, auto d) {
+    using S = decltype(s);
+    using D = decltype(d);
+    k_convolve<S, D><<<g, kBlock, 0, st>>>((D*)dst.ptr, (const S*)src.ptr, (const float*)kern.ptr, dims(src),
+                                           dims(kern), dims(dst), r, p.rte);
+  });
+  if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "convolve: pixel types %d -> %d", src.dt, dst.dt);
+  count_launch();
+  return check_launch("convolve");
 }
 
 clk_status direct_greater_constant(const Image& dst, const Image& src, float scalar, Range r, cudaStream_t st) {

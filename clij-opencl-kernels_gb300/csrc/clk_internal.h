@@ -108,6 +108,8 @@ enum StencilKind {
 };
 clk_status direct_stencil(StencilKind kind, const Image& dst, const Image& src, Range r, const Policy& p,
                           cudaStream_t st);
+clk_status direct_convolve(const Image& dst, const Image& src, const Image& kern, Range r, const Policy& p,
+                           cudaStream_t st);
 // min / max / mean over the radius-1 and radius-2 spheres (disks when planar
 // or 2-D) for 8/16-bit pixels, src type = dst type (clk_sphere_rank.cu)
 clk_status fast_sphere_rank(RankOp op, bool planar, const Image& dst, const Image& src, const MedianNbhd& m,
@@ -116,6 +118,8 @@ clk_status fast_sphere_rank(RankOp op, bool planar, const Image& dst, const Imag
 // (clk_pointwise.cu); CLK_UNSUPPORTED_DTYPE where extents or alignment differ
 clk_status fast_pointwise(bool greater, const Image& dst, const Image& src, float scalar, const Policy& p,
                           cudaStream_t st);
+// gradient along axis 0/1/2 over whole rows (width a multiple of 8, aligned)
+clk_status fast_gradient(int axis, const Image& dst, const Image& src, const Policy& p, cudaStream_t st);
 clk_status direct_morph(bool erode, bool sphere, const Image& dst, const Image& src, Range r, const Policy& p,
                         cudaStream_t st, bool planar = false);
 clk_status direct_sobel(const Image& dst, const Image& src, Range r, const Policy& p, cudaStream_t st);

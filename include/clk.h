@@ -114,6 +114,22 @@ typedef struct clk_define {
  *   dilate_box_{2d,3d}, dilate_sphere_{2d,3d}   (src, dst)
  *                                    erode_box_3d_x.cl:3-6
  *   sobel_{2d,3d}                    (dst, src)   sobel_3d_x.cl:3-7
+ *   and the neighbourhood filters either side of them:
+ *   minimum_sphere_{2d,3d}, maximum_sphere_{2d,3d}, mean_sphere_{2d,3d}
+ *                                    (dst, src, int Nx, int Ny[, int Nz])
+ *                                    minimum_sphere_3d_x.cl:3-10
+ *   minimum/maximum/mean_slice_by_slice_sphere_3d,
+ *   median_slice_by_slice_box_3d, median_slice_by_slice_sphere_3d
+ *                                    (dst, src, int Nx, int Ny)
+ *                                    minimum_slice_by_slice_sphere_3d_x.cl:3-9
+ *   erode/dilate_box/sphere_slice_by_slice_3d   (src, dst)
+ *   greater_constant_{2d,3d}         (src1, float scalar, dst)
+ *                                    greater_constant_3d_x.cl:3-7
+ *   copy_{2d,3d}                     (dst, src)   copy_3d_x.cl:3-6
+ *   gradient_x_2d, gradient_y_2d, gradient_{x,y,z}_3d   (dst, src)
+ *   laplace_box_{2d,3d}, laplace_diamond_{2d,3d}        (dst, src)
+ *   convolve_{2d,3d}                 (src, kernelImage, dst); the kernel
+ *                                    image is float   convolve_3d_x.cl:1-5
  * global: the global work size; voxels [0,global[0]) x [0,global[1]) x
  *   [0,global[2]) of dst are written (the reference's NDRange); it must not
  *   exceed dst's extent.  NULL means "dst's extent".  Reads of src are

@@ -58,6 +58,7 @@ KERNELS = [
     "greater_constant_2d", "greater_constant_3d", "copy_2d", "copy_3d",
     "gradient_x_2d", "gradient_y_2d", "gradient_x_3d", "gradient_y_3d", "gradient_z_3d",
     "laplace_box_2d", "laplace_box_3d", "laplace_diamond_2d", "laplace_diamond_3d",
+    "convolve_2d", "convolve_3d",
 ]
 # pixel types in clk_dtype order (include/clk.h)
 DTYPES = [("u8", "uint8_t"), ("i8", "int8_t"), ("u16", "uint16_t"),
@@ -134,9 +135,11 @@ def generate(reference: Path = DEFAULT_REFERENCE) -> list[Path]:
                         args.append(f"c->ia[{ni}]"); ni += 1
                     else:
                         args.append(f"c->fa[{nf}]"); nf += 1
+                kimg = (" clkcl::clk_img<float> kernelImage{(float*)c->kimg, c->kw, c->kh, c->kd};"
+                        if any(ident == "kernelImage" for _, ident in params) else "")
                 body.append(
                     f"  case {si * 5 + di}: {{ clkcl::clk_img<{st}> src{{({st}*)c->src, c->sw, c->sh, c->sd}};"
-                    f" clkcl::clk_img<{dt}> dst{{({dt}*)c->dst, c->dw, c->dh, c->dd}};"
+                    f" clkcl::clk_img<{dt}> dst{{({dt}*)c->dst, c->dw, c->dh, c->dd}};{kimg}"
                     f" clkref_loop(c, [&] {{ {ns}::{k}({', '.join(args)}); }}); return 0; }}")
         body.append("  default: return -1;\n  }\n}")
         out = GEN_DIR / f"{k}.cpp"

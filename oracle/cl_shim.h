@@ -134,6 +134,13 @@ struct clk_sobel_array {
 #define IMAGE_src_PIXEL_TYPE SRC_T
 #define IMAGE_dst_PIXEL_TYPE DST_T
 #define READ_src_IMAGE(img, smp, ...) clk_read(img, __VA_ARGS__)
+// convolve_{2d,3d}_x.cl: a float kernel image and the untyped accessors
+#define IMAGE_kernelImage_TYPE clk_img<float>
+#define READ_IMAGE(img, smp, ...) clk_read(img, __VA_ARGS__)
+#define WRITE_IMAGE(img, ...) clk_write(img, __VA_ARGS__)
+#define GET_IMAGE_WIDTH(img) ((img).w)
+#define GET_IMAGE_HEIGHT(img) ((img).h)
+#define GET_IMAGE_DEPTH(img) ((img).d)
 // greater_constant_{2d,3d}_x.cl name their input src1
 #define IMAGE_src1_TYPE clk_img<SRC_T>
 #define IMAGE_src1_PIXEL_TYPE SRC_T

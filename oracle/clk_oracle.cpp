@@ -443,6 +443,30 @@ static void laplace_box3d(const Vol& dst, const Vol& src, const int g[3], int fl
   }
 }
 
+// convolve_{2d,3d}_x.cl:17-31: c = kernel extent / 2 per axis; for x, y, z
+// in -c..c: sum = sum + (float)kernel(c + offset) * (float)src(coord + offset),
+// both reads clamped; CONVERT(sum).
+template <class S, class D>
+static void convolve(const Vol& dst, const Vol& src, const float* kern, const int kshape[3], const int g[3],
+                     int flags, int nt) {
+  const int cx = kshape[0] / 2, cy = kshape[1] / 2, cz = kshape[2] / 2;
+  const Vol K{(void*)kern, F32, kshape[0], kshape[1], kshape[2]};
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (long zy = 0; zy < (long)g[2] * g[1]; ++zy) {
+    const int z = (int)(zy / g[1]), y = (int)(zy % g[1]);
+    for (int x = 0; x < g[0]; ++x) {
+      float sum = 0;
+      for (int a = -cx; a <= cx; ++a)
+        for (int b = -cy; b <= cy; ++b)
+          for (int c = -cz; c <= cz; ++c) {
+            const float kv = kern[vidx(K, cx + a, cy + b, cz + c)];
+            sum = sum + kv * (float)readx<S>(src, x + a, y + b, z + c);
+          }
+      ((D*)dst.p)[(long)x + (long)dst.w * ((long)y + (long)dst.h * z)] = convert_sat<D>((double)sum, flags);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- dispatch
 template <class F> static int with_types(int sdt, int ddt, F f) {
   auto d = [&](auto s) -> int {
@@ -583,6 +607,18 @@ int clko_execute(const char* kernel, int sdt, int ddt, const void* src, const in
       return 0;
     });
   return -1;
+}
+
+// convolve_{2d,3d}: src * a float kernel image over global range g.
+int clko_convolve(int sdt, int ddt, const void* src, const int sshape[3], const float* kern, const int kshape[3],
+                  void* dst, const int dshape[3], const int g[3], int flags, int nthreads) {
+  const int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+  Vol S{(void*)src, sdt, sshape[0], sshape[1], sshape[2]};
+  Vol D{dst, ddt, dshape[0], dshape[1], dshape[2]};
+  return with_types(sdt, ddt, [&](auto s, auto d) {
+    convolve<decltype(s), decltype(d)>(D, S, kern, kshape, g, flags, nt);
+    return 0;
+  });
 }
 
 // Orchestrated separable filter: passes X, Y(, Z) with dst-typed

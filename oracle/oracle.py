@@ -47,6 +47,7 @@ KERNELS = [
     "greater_constant_2d", "greater_constant_3d", "copy_2d", "copy_3d",
     "gradient_x_2d", "gradient_y_2d", "gradient_x_3d", "gradient_y_3d", "gradient_z_3d",
     "laplace_box_2d", "laplace_box_3d", "laplace_diamond_2d", "laplace_diamond_3d",
+    "convolve_2d", "convolve_3d",
 ]
 
 
@@ -92,7 +93,8 @@ class _RefCall(C.Structure):
     _fields_ = [("src", C.c_void_p), ("sw", C.c_int), ("sh", C.c_int), ("sd", C.c_int),
                 ("dst", C.c_void_p), ("dw", C.c_int), ("dh", C.c_int), ("dd", C.c_int),
                 ("gx", C.c_int), ("gy", C.c_int), ("gz", C.c_int),
-                ("ia", C.c_int * 4), ("fa", C.c_float * 4), ("nthreads", C.c_int)]
+                ("ia", C.c_int * 4), ("fa", C.c_float * 4), ("nthreads", C.c_int),
+                ("kimg", C.c_void_p), ("kw", C.c_int), ("kh", C.c_int), ("kd", C.c_int)]
 
 
 def ref_available() -> bool:
@@ -127,9 +129,13 @@ def _fa(v):
 
 
 def execute(kernel: str, src: np.ndarray, dst_dtype, ints=(), floats=(), global_range=None,
-            flags: int = 0, impl: str = "port", nthreads: int = 0, dst: np.ndarray | None = None) -> np.ndarray:
-    """One launch of `kernel` on the CPU; returns dst (fresh zeros unless given)."""
+            flags: int = 0, impl: str = "port", nthreads: int = 0, dst: np.ndarray | None = None,
+            kernel_image: np.ndarray | None = None) -> np.ndarray:
+    """One launch of `kernel` on the CPU; returns dst (fresh zeros unless given).
+    kernel_image: the float32 kernel of convolve_{2d,3d}."""
     src = np.ascontiguousarray(src)
+    if kernel.startswith("convolve"):
+        return _convolve(kernel, src, dst_dtype, kernel_image, global_range, flags, impl, nthreads, dst)
     if dst is None:
         dst = np.zeros(src.shape, dtype=dst_dtype)
     sx, dx = _xyz(src), _xyz(dst)
@@ -211,3 +217,29 @@ def median_offsets(sphere: bool, ndim: int, Nx: int, Ny: int, Nz: int = 1) -> np
 
 def nthreads_default() -> int:
     return os.cpu_count() or 1
+
+
+def _convolve(kernel, src, dst_dtype, kimg, global_range, flags, impl, nthreads, dst):
+    if kimg is None:
+        raise ValueError("convolve needs kernel_image")
+    kimg = np.ascontiguousarray(kimg, dtype=np.float32)
+    if dst is None:
+        dst = np.zeros(src.shape, dtype=dst_dtype)
+    sx, dx, kx = _xyz(src), _xyz(dst), _xyz(kimg)
+    g = list(global_range) if global_range is not None else dx
+    sdt, ddt = dtype_code(src.dtype), dtype_code(dst.dtype)
+    if impl == "ref":
+        call = _RefCall(src.ctypes.data, *sx, dst.ctypes.data, *dx, *g, _ia(()), _fa(()), nthreads,
+                        kimg.ctypes.data, *kx)
+        rc = getattr(ref(), f"clkref_{kernel}")(sdt, ddt, C.byref(call))
+    else:
+        i3 = lambda v: (C.c_int * 3)(*v)  # noqa: E731
+        lib = port()
+        lib.clko_convolve.argtypes = [C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.c_void_p,
+                                      C.POINTER(C.c_int), C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.c_int, C.c_int]
+        rc = lib.clko_convolve(sdt, ddt, src.ctypes.data, i3(sx), kimg.ctypes.data, i3(kx), dst.ctypes.data,
+                               i3(dx), i3(g), flags, nthreads)
+    if rc != 0:
+        raise RuntimeError(f"oracle {impl} {kernel} failed ({rc})")
+    return dst

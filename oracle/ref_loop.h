@@ -20,6 +20,8 @@ struct clkref_call {
   int ia[4];
   float fa[4];
   int nthreads;
+  void* kimg;  // convolve: the float kernel image
+  int kw, kh, kd;
 };
 }
 

@@ -50,14 +50,25 @@ def main() -> None:
     rng = np.random.default_rng(20240601)
     arrays, index = {}, []
 
-    def add(kind, kernel, sdt, ddt, params, a, out):
+    def add(kind, kernel, sdt, ddt, params, a, out, kimg=None):
         key = f"c{len(index):04d}"
         arrays[key + "_in"] = a
         arrays[key + "_out"] = out
+        if kimg is not None:
+            arrays[key + "_k"] = kimg
         index.append({"key": key, "kind": kind, "kernel": kernel, "src": sdt, "dst": ddt, "params": params})
 
     for k in O.KERNELS:
         is2 = k.endswith("2d")
+        if k.startswith("convolve"):
+            for shp in ([(10, 13), (1, 6)] if is2 else [(5, 7, 9), (1, 3, 8)]):
+                for sdt, ddt in PAIRS_SEP:
+                    a = image(rng, shp, sdt)
+                    for ks in (((3, 3), (4, 2)) if is2 else ((3, 3, 3), (2, 3, 4))):
+                        kimg = rng.standard_normal(ks).astype(np.float32)
+                        out = O.execute(k, a, NP[ddt], impl="ref", kernel_image=kimg)
+                        add("convolve", k, sdt, ddt, {"kernel_shape": list(ks)}, a, out, kimg)
+            continue
         shapes = [(10, 13), (1, 6)] if is2 else [(5, 7, 9), (1, 3, 8)]
         if "slice_by_slice" in k and not k.startswith(("erode", "dilate")):
             pairs = PAIRS_MEDIAN if k.startswith("median") else PAIRS_SEP

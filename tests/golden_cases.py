@@ -12,6 +12,8 @@ def load():
     z = np.load(PATH)
     index = json.loads(bytes(z["index"]).decode())
     for c in index:
+        if c["key"] + "_k" in z:  # convolve: its float kernel image
+            c = dict(c, kernel_image=z[c["key"] + "_k"])
         yield c, z[c["key"] + "_in"], z[c["key"] + "_out"]
 
 

@@ -83,7 +83,7 @@ def _params(kernel):
     return [{}]
 
 
-KERNELS = __import__("oracle.oracle", fromlist=["KERNELS"]).KERNELS
+KERNELS = [k for k in __import__("oracle.oracle", fromlist=["KERNELS"]).KERNELS if not k.startswith("convolve")]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
@@ -91,7 +91,8 @@ def test_execute_matches_oracle_every_dtype_pair(clk, oracle, kernel):
     rng = np.random.default_rng(abs(hash(kernel)) % 2**32)
     is2 = kernel.endswith("2d")
     morph = kernel.startswith(("erode", "dilate"))
-    for shp in (((17, 33), (1, 7)) if is2 else ((9, 17, 33), (1, 5, 6), (4, 1, 1))):
+    # widths that are multiples of 16 take the vectorised fast paths
+    for shp in (((17, 33), (1, 7), (9, 16)) if is2 else ((9, 17, 33), (1, 5, 6), (4, 1, 1), (3, 9, 16))):
         for sdt in DTYPES:
             for ddt in DTYPES:
                 if kernel.startswith("median") and sdt != ddt:
@@ -104,6 +105,22 @@ def test_execute_matches_oracle_every_dtype_pair(clk, oracle, kernel):
                     want = oracle.execute(kernel, a, ddt, ints, floats)
                     got = run_execute(clk, kernel, a, ddt, p, defines=EXACT)
                     assert got.tobytes() == want.tobytes(), (kernel, shp, np.dtype(sdt), np.dtype(ddt), p)
+
+
+@pytest.mark.parametrize("kernel", ["convolve_2d", "convolve_3d"])
+def test_convolve_matches_oracle(clk, oracle, kernel):
+    rng = np.random.default_rng(82)
+    is2 = kernel.endswith("2d")
+    kshapes = ((3, 3), (5, 3), (4, 4), (1, 1)) if is2 else ((3, 3, 3), (5, 3, 1), (4, 2, 3), (1, 1, 1))
+    for shp in (((17, 33), (1, 7)) if is2 else ((9, 17, 33), (1, 5, 6))):
+        for sdt in DTYPES:
+            for ddt in DTYPES:
+                a = random_image(rng, shp, sdt)
+                for ks in kshapes:
+                    k = rng.standard_normal(ks).astype(np.float32)
+                    want = oracle.execute(kernel, a, ddt, kernel_image=k)
+                    got = run_execute(clk, kernel, a, ddt, {"kernelImage": dev(k)})
+                    assert got.tobytes() == want.tobytes(), (kernel, shp, np.dtype(sdt), np.dtype(ddt), ks)
 
 
 @pytest.mark.parametrize("kernel", ["sobel_2d", "sobel_3d"])
@@ -141,7 +158,9 @@ def test_golden_fixtures_on_gpu(clk):
     n = 0
     for c, a, want in golden_cases.load():
         dt = golden_cases.NP[c["dst"]]
-        if c["kind"] == "execute":
+        if c["kind"] == "convolve":
+            got = run_execute(clk, c["kernel"], a, dt, {"kernelImage": dev(c["kernel_image"])}, defines=EXACT)
+        elif c["kind"] == "execute":
             got = run_execute(clk, c["kernel"], a, dt, c["params"], defines=EXACT)
         else:
             d = empty(a.shape, dt)

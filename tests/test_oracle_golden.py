@@ -13,7 +13,9 @@ def test_port_matches_golden(oracle):
     n = 0
     for c, a, want in golden_cases.load():
         dt = golden_cases.NP[c["dst"]]
-        if c["kind"] == "execute":
+        if c["kind"] == "convolve":
+            got = oracle.execute(c["kernel"], a, dt, kernel_image=c["kernel_image"])
+        elif c["kind"] == "execute":
             ints, floats = golden_cases.split_params(c["params"])
             got = oracle.execute(c["kernel"], a, dt, ints, floats)
         else:

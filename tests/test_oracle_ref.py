@@ -41,7 +41,8 @@ def _ref_or_skip(O):
         pytest.skip("oracle/_ref not built (reference checkout absent)")
 
 
-@pytest.mark.parametrize("kernel", [k for k in __import__("oracle.oracle", fromlist=["KERNELS"]).KERNELS])
+@pytest.mark.parametrize("kernel", [k for k in __import__("oracle.oracle", fromlist=["KERNELS"]).KERNELS
+                                    if not k.startswith("convolve")])
 def test_port_matches_reference(oracle, kernel):
     O = oracle
     _ref_or_skip(O)
@@ -83,3 +84,23 @@ def test_separable_orchestration_matches_reference(oracle, kernel):
             r = O.separable(kernel, a, ddt, N, s, impl="ref")
             p = O.separable(kernel, a, ddt, N, s, impl="port")
             assert r.tobytes() == p.tobytes(), (kernel, np.dtype(sdt), np.dtype(ddt), N, s)
+
+
+@pytest.mark.parametrize("kernel", ["convolve_2d", "convolve_3d"])
+def test_convolve_port_matches_reference(oracle, kernel):
+    """convolve takes a float kernel image: odd, even and unit extents."""
+    O = oracle
+    _ref_or_skip(O)
+    rng = np.random.default_rng(81)
+    is2 = kernel.endswith("2d")
+    shapes = ((9, 11), (1, 5)) if is2 else ((7, 9, 11), (1, 4, 5))
+    kshapes = ((3, 3), (5, 3), (4, 4), (1, 1)) if is2 else ((3, 3, 3), (5, 3, 1), (4, 2, 3), (1, 1, 1))
+    for shp in shapes:
+        for sdt in DTYPES:
+            for ddt in DTYPES:
+                a = random_image(rng, shp, sdt)
+                for ks in kshapes:
+                    k = rng.standard_normal(ks).astype(np.float32)
+                    r = O.execute(kernel, a, ddt, impl="ref", kernel_image=k)
+                    p = O.execute(kernel, a, ddt, impl="port", kernel_image=k)
+                    assert r.tobytes() == p.tobytes(), (kernel, shp, np.dtype(sdt), np.dtype(ddt), ks)
