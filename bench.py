@@ -47,6 +47,9 @@ NCU_DRAM_BYTES_PER_VOXEL = {
     "gaussian_blur s(3,3,1.5)": 5.88, "mean_box r(5,5,2)": 3.95, "minimum_box r(5,5,2)": 3.98,
     "median_box r1": 3.74, "median_sphere r2": 3.74, "sobel_3d": 5.66,
 }
+# The selection networks are bound by the min/max (ALU) pipe, not by DRAM:
+# its busy fraction from the same capture.
+NCU_ALU_PIPE_BUSY = {"median_box r1": 0.78, "median_sphere r2": 0.82}
 
 
 def suite_spec():
@@ -126,11 +129,25 @@ def dist():
     return ws, rank, local
 
 
+def replicas_value(local_ms: float, voxels_per_step: int, steps: int, ws: int, device=None):
+    """Replicas only (the path shards by stack, no exchange step): every
+    rank filters its own stack; the job's time is the slowest rank's and its
+    throughput all ranks' voxels over that time.  Returns (max_ms, Gvoxel/s)."""
+    ms = local_ms
+    if ws > 1:
+        import torch
+        import torch.distributed as tdist
+        t = torch.tensor([local_ms], dtype=torch.float64, device=device)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, ws * voxels_per_step * steps / (ms * 1e-3) / 1e9
+
+
 def run_reference(args):
     """The reference kernels on the host cores, on a bounded sample."""
     ws, rank, _ = dist()
-    if rank != 0:
-        return
+    if rank != 0:  # rank 0 alone times the host cores; the others exit 0 without work
+        return 0
     import numpy as np
     import torch
 
@@ -669,10 +686,7 @@ def main():
         torch.cuda.synchronize()
     launches = clk.launch_count() - launches0
     total_ms = t_begin.elapsed_time(t_end)
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms, value = replicas_value(total_ms, V * len(spec), args.steps, ws, device=dev)
     per = {}
     for name, kind, kernel, params, srcn, ddt, bpv in spec:
         ms = statistics.mean(a.elapsed_time(b) for a, b in ev[name])
@@ -681,7 +695,6 @@ def main():
                      "hbm_frac": round(gbs / peak, 4), "bytes_per_voxel": bpv}
     dom = max(per, key=lambda n: per[n]["ms"])
     dom_gbs = V * per[dom]["bytes_per_voxel"] / (per[dom]["ms"] * 1e-3) / 1e9
-    value = ws * V * len(spec) * args.steps / (total_ms * 1e-3) / 1e9
 
     e2e = None
     if not args.no_e2e:
@@ -761,7 +774,10 @@ def main():
                          "unit": "GB/s", "frac": round(dom_gbs / peak, 4), "peak_kind": peak_kind,
                          "traffic": (round(NCU_DRAM_BYTES_PER_VOXEL[dom] * V) if dom in NCU_DRAM_BYTES_PER_VOXEL
                                      else None),
-                         "algorithmic_bytes": int(V * per[dom]["bytes_per_voxel"])},
+                         "algorithmic_bytes": int(V * per[dom]["bytes_per_voxel"]),
+                         **({"alu_pipe_busy": NCU_ALU_PIPE_BUSY[dom],
+                             "note": "selection network: bound by the min/max (ALU) pipe, not HBM"}
+                            if dom in NCU_ALU_PIPE_BUSY else {})},
             "gpu_launches": launches,
             "clocks": clocks.result,
             "e2e": e2e,
