@@ -44,12 +44,12 @@ METRIC = "Gvoxel/s (plain filter suite, 1024x1024x256)"
 # capture summarised in profiles/sep2_sobel_median_kernels_1024x1024x128_u16.md
 # (a 1024x1024x128 slab of the same stack; traffic scales with the voxels).
 NCU_DRAM_BYTES_PER_VOXEL = {
-    "gaussian_blur s(3,3,1.5)": 5.88, "mean_box r(5,5,2)": 3.95, "minimum_box r(5,5,2)": 3.98,
-    "median_box r1": 3.74, "median_sphere r2": 3.74, "sobel_3d": 5.66,
+    "gaussian_blur s(3,3,1.5)": 5.92, "mean_box r(5,5,2)": 3.89, "minimum_box r(5,5,2)": 3.98,
+    "median_box r1": 3.74, "median_sphere r2": 3.73, "sobel_3d": 5.65,
 }
 # The selection networks are bound by the min/max (ALU) pipe, not by DRAM:
 # its busy fraction from the same capture.
-NCU_ALU_PIPE_BUSY = {"median_box r1": 0.78, "median_sphere r2": 0.82}
+NCU_ALU_PIPE_BUSY = {"median_box r1": 0.78, "median_sphere r2": 0.74}
 
 
 def suite_spec():
@@ -127,6 +127,25 @@ def dist():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def gpu_local_cpus(index: int):
+    """The CPUs of the GPU's NUMA node (sysfs local_cpulist of its PCI
+    device), or None.  Host buffers first touched from them live in the memory
+    next to the GPU's host link."""
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(index), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=20).stdout.strip()
+        dom, rest = bus.split(":", 1)
+        text = Path(f"/sys/bus/pci/devices/{int(dom, 16):04x}:{rest.lower()}/local_cpulist").read_text().strip()
+        cpus = set()
+        for part in text.split(","):
+            lo, _, hi = part.partition("-")
+            cpus.update(range(int(lo), int(hi or lo) + 1))
+        cpus &= os.sched_getaffinity(0)
+        return cpus or None
+    except Exception:
+        return None
 
 
 def replicas_value(local_ms: float, voxels_per_step: int, steps: int, ws: int, device=None):
@@ -598,6 +617,12 @@ def main():
     ap.add_argument("--full-sample", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-pull", default="zero-copy", choices=["zero-copy", "copy"],
+                    help="how results reach host memory in the e2e run: the filters store into pinned host "
+                         "images (zero-copy) or write device images that copy engines then pull")
+    ap.add_argument("--e2e-push", default="kernel", choices=["kernel", "copy"],
+                    help="how the input stack and mask reach the device in the e2e run: copy_3d kernels reading "
+                         "the pinned host images (kernel) or copy-engine copies")
     ap.add_argument("--shape", default="", help="suite stack as z,y,x (default 256,1024,1024)")
     ap.add_argument("--filters", default="", help="regex selecting suite filters by name")
     ap.add_argument("--workload", default="suite", choices=["suite", "batch", "serve", "large", "neighbours"],
@@ -699,14 +724,26 @@ def main():
     e2e = None
     if not args.no_e2e:
         # The same suite from pinned host buffers, pipelined the way a caller
-        # would: host->device copies of step k+1, the filters of step k and
-        # device->host copies of step k's outputs run on three streams, with
-        # two sets of device buffers.  Every byte still crosses the link.
+        # would: the host->device copy of step k+1's stack and mask (copy
+        # engine, two device input sets) overlaps the filters of step k.  The
+        # results reach host memory either by the filters storing straight
+        # into pinned host images over the host link (zero-copy, the
+        # default: clk_host_image_pointer) or by device outputs that a third
+        # stream pulls with copy engines.  Every byte crosses the link inside
+        # the timed region either way.
+        saved_aff = os.sched_getaffinity(0)
+        local_cpus = gpu_local_cpus(local)
+        if local_cpus:  # pinned pages first-touched next to the GPU
+            os.sched_setaffinity(0, local_cpus)
+        zero_copy = args.e2e_pull == "zero-copy"
+        push_kernel = args.e2e_push == "kernel"
         h_img = img.cpu().pin_memory()
         h_mask = mask.cpu().pin_memory()
         h_out = {n: torch.empty(shape, dtype=o.dtype).pin_memory() for n, o in outs.items()}
+        for t in h_out.values():
+            t.zero_()
         d_in = [{"img": torch.empty_like(img), "mask": torch.empty_like(mask)} for _ in range(2)]
-        d_out = [{n: torch.empty_like(o) for n, o in outs.items()} for _ in range(2)]
+        d_out = None if zero_copy else [{n: torch.empty_like(o) for n, o in outs.items()} for _ in range(2)]
         cs, hs, ds = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
         ev_in = [torch.cuda.Event() for _ in range(2)]
         ev_in_free = [torch.cuda.Event() for _ in range(2)]
@@ -719,37 +756,55 @@ def main():
             with torch.cuda.stream(hs):
                 if used[b]:
                     hs.wait_event(ev_in_free[b])
-                d_in[b]["img"].copy_(h_img, non_blocking=True)
-                d_in[b]["mask"].copy_(h_mask, non_blocking=True)
+                if push_kernel:
+                    clk.execute("copy_3d", {"src": h_img, "dst": d_in[b]["img"]}, stream=hs)
+                    clk.execute("copy_3d", {"src": h_mask, "dst": d_in[b]["mask"]}, stream=hs)
+                else:
+                    d_in[b]["img"].copy_(h_img, non_blocking=True)
+                    d_in[b]["mask"].copy_(h_mask, non_blocking=True)
                 ev_in[b].record(hs)
             cs.wait_event(ev_in[b])
             for name, kind, kernel, params, srcn, ddt, bpv in spec:
+                if zero_copy:
+                    run(name, kind, kernel, params, srcn, d_in[b][srcn], h_out[name], st=cs)
+                    continue
                 if used[b]:
                     cs.wait_event(ev_out_free[b][name])
                 run(name, kind, kernel, params, srcn, d_in[b][srcn], d_out[b][name], st=cs)
                 ev_out[b][name].record(cs)
             ev_in_free[b].record(cs)
-            with torch.cuda.stream(ds):
-                for name in outs:
-                    ds.wait_event(ev_out[b][name])
-                    h_out[name].copy_(d_out[b][name], non_blocking=True)
-                    ev_out_free[b][name].record(ds)
+            if not zero_copy:
+                with torch.cuda.stream(ds):
+                    for name in outs:
+                        ds.wait_event(ev_out[b][name])
+                        h_out[name].copy_(d_out[b][name], non_blocking=True)
+                        ev_out_free[b][name].record(ds)
             used[b] = True
 
         e2e_step(0)
         e2e_step(1)
         torch.cuda.synchronize()
+        l0 = clk.launch_count()
         t0 = time.perf_counter()
         for k in range(args.steps):
             e2e_step(k)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
+        os.sched_setaffinity(0, saved_aff)
         e2e = {"value": round(V * len(spec) * args.steps / dt / 1e9, 3), "unit": "Gvoxel/s",
                "h2d_bytes_per_step": img.numel() * 2 + mask.numel(),
                "d2h_bytes_per_step": sum(o.numel() * o.element_size() for o in outs.values()),
                "ms_per_step": round(dt * 1e3 / args.steps, 2),
-               "path": "pinned host stack + mask -> device, clk C-ABI calls, all outputs -> pinned host; "
-                       "copies and filters pipelined on three streams"}
+               "gpu_launches": clk.launch_count() - l0,
+               "push": args.e2e_push, "pull": args.e2e_pull,
+               "path": ("pinned host stack + mask -> device (" + ("copy_3d kernels" if push_kernel else "copy engine")
+                        + "), clk C-ABI calls " + ("storing every output straight into pinned host images (zero-copy "
+                                                   "over the host link)" if zero_copy else
+                                                   "writing device outputs that copy engines pull to pinned host")
+                        + "; the next step's input copy overlaps the filters")}
+        if zero_copy:  # the host images hold the filters' results
+            ok = all(torch.equal(h_out[n], outs[n].cpu()) for n in outs) if args.steps > 0 else True
+            e2e["host_results_match_device"] = bool(ok)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

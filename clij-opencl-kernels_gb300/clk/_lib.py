@@ -63,7 +63,7 @@ EXPORTS = ["clk_execute", "clk_separable", "clk_separable_noalloc", "clk_morphol
            "clk_batch_run", "clk_batch_run_plain", "clk_batch_run_per_kernel", "clk_batch_launches", "clk_batch_destroy", "clk_server_create",
            "clk_server_submit", "clk_server_wait", "clk_server_drain", "clk_server_get_stats",
            "clk_server_destroy", "clk_supported", "clk_last_error_string", "clk_version",
-           "clk_kernel_count", "clk_kernel_name", "clk_launch_count"]
+           "clk_kernel_count", "clk_kernel_name", "clk_launch_count", "clk_host_image_pointer"]
 
 _lib = None
 
@@ -120,6 +120,8 @@ def load() -> C.CDLL:
     lib.clk_kernel_name.argtypes = [C.c_int]
     lib.clk_kernel_name.restype = C.c_char_p
     lib.clk_launch_count.restype = C.c_uint64
+    lib.clk_host_image_pointer.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    lib.clk_host_image_pointer.restype = C.c_int
     _lib = lib
     return lib
 

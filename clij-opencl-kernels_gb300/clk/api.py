@@ -14,7 +14,9 @@ Two levels, as in the reference's ecosystem:
 
 Images are CUDA tensors (torch is only the device-memory container here),
 C-contiguous, shape (depth, height, width) or (height, width): x fastest,
-exactly the reference's buffer layout.  Pixel types: uint8, int8, uint16,
+exactly the reference's buffer layout.  A pinned host tensor is accepted too
+(zero-copy: the kernel stores its output straight into host memory over the
+host link, which fuses the pull of the result into the filter).  Pixel types: uint8, int8, uint16,
 int16, float32.
 """
 from __future__ import annotations
@@ -42,15 +44,34 @@ def torch_dtype(code: int) -> torch.dtype:
     return _TORCH[code]
 
 
+def host_image_pointer(t: torch.Tensor) -> int:
+    """The address under which kernels reach a pinned host tensor
+    (clk_host_image_pointer); BAD_ARG for pageable memory."""
+    lib = L.load()
+    out = C.c_void_p()
+    L.check(lib.clk_host_image_pointer(C.c_void_p(t.data_ptr()), C.byref(out)))
+    return int(out.value)
+
+
 def image_of(t: torch.Tensor) -> L.clk_image:
-    if not isinstance(t, torch.Tensor) or not t.is_cuda:
-        raise L.ClkError(L.BAD_ARG, "images must be CUDA tensors")
+    """A CUDA tensor, or a pinned host tensor (zero-copy: the kernel reads or
+    writes host memory over the host link; meant for outputs)."""
+    if not isinstance(t, torch.Tensor):
+        raise L.ClkError(L.BAD_ARG, "images must be CUDA tensors or pinned host tensors")
     if not t.is_contiguous():
         raise L.ClkError(L.BAD_ARG, "images must be C-contiguous (x fastest)")
+    if t.dim() not in (2, 3):
+        raise L.ClkError(L.BAD_ARG, f"images are 2-D or 3-D, got shape {tuple(t.shape)}")
+    if t.is_cuda:
+        ptr = t.data_ptr()
+    elif t.device.type == "cpu" and t.is_pinned():
+        ptr = host_image_pointer(t)
+    else:
+        raise L.ClkError(L.BAD_ARG, "images must be CUDA tensors or pinned host tensors (pin_memory())")
     if t.dim() == 2:
-        return L.clk_image(t.data_ptr(), dtype_code(t.dtype), 2, t.shape[1], t.shape[0], 1)
+        return L.clk_image(ptr, dtype_code(t.dtype), 2, t.shape[1], t.shape[0], 1)
     if t.dim() == 3:
-        return L.clk_image(t.data_ptr(), dtype_code(t.dtype), 3, t.shape[2], t.shape[1], t.shape[0])
+        return L.clk_image(ptr, dtype_code(t.dtype), 3, t.shape[2], t.shape[1], t.shape[0])
     raise L.ClkError(L.BAD_ARG, f"images are 2-D or 3-D, got shape {tuple(t.shape)}")
 
 

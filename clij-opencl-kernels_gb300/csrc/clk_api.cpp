@@ -628,6 +628,22 @@ int clk_supported(const char* kernel_name, int32_t src_dtype, int32_t dst_dtype,
   return 1;
 }
 
+clk_status clk_host_image_pointer(const void* host_ptr, void** device_ptr) {
+  t_error.clear();
+  if (!host_ptr || !device_ptr) return fail(CLK_BAD_ARG, "clk_host_image_pointer: null pointer");
+  *device_ptr = nullptr;
+  if (const clk_status st = device_ready(); st != CLK_OK) return st;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, host_ptr) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(CLK_BAD_ARG, "clk_host_image_pointer: %p is not memory known to CUDA", host_ptr);
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer)
+    return fail(CLK_BAD_ARG, "clk_host_image_pointer: %p is not page-locked host memory", host_ptr);
+  *device_ptr = a.devicePointer;
+  return CLK_OK;
+}
+
 const char* clk_last_error_string(void) { return t_error.c_str(); }
 
 const char* clk_version(void) {

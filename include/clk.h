@@ -285,6 +285,18 @@ clk_status clk_server_drain(clk_server* server, int32_t timeout_ms);
 clk_status clk_server_get_stats(clk_server* server, clk_server_stats* out);
 void clk_server_destroy(clk_server* server);
 
+/* The address under which kernels reach a page-locked host buffer (memory
+ * from cudaHostAlloc / cudaMallocHost or registered with cudaHostRegister,
+ * e.g. a pinned torch tensor), for use as a clk_image ptr.  A kernel given
+ * it as dst stores its output straight into host memory over the host link
+ * (zero-copy: no device copy of the output and no separate device->host
+ * transfer); as src every read crosses the link, so inputs of neighbourhood
+ * filters are better copied to the device first.  CLK_BAD_ARG if host_ptr is
+ * not page-locked host memory.  Replaces the pull of a result image
+ * (CLIc's pull / clij's pull of a device buffer to a host array) for
+ * callers that keep results on the host. */
+clk_status clk_host_image_pointer(const void* host_ptr, void** device_ptr);
+
 /* Is kernel_name available for this (src, dst) pixel-type pair and ndim?
  * Returns 1 if yes, 0 if no. */
 int clk_supported(const char* kernel_name, int32_t src_dtype,

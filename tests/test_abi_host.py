@@ -164,3 +164,21 @@ def test_supported(L):
     assert lib.clk_supported(b"median_box_3d", 2, 2, 2) == 0
     assert lib.clk_supported(b"sobel_3d", 2, 4, 3) == 1
     assert lib.clk_supported(b"nope", 2, 4, 3) == 0
+
+
+def test_host_image_pointer_validation(L):
+    out = C.c_void_p()
+    assert L.load().clk_host_image_pointer(None, C.byref(out)) == L.BAD_ARG
+    import torch
+    if not torch.cuda.is_available():
+        buf = (C.c_char * 64)()
+        assert L.load().clk_host_image_pointer(C.cast(buf, C.c_void_p), C.byref(out)) == L.NO_DEVICE
+
+
+def test_pageable_host_tensors_are_rejected():
+    import torch
+    import clk
+    from clk import _lib as Lm
+    with pytest.raises(Lm.ClkError) as e:
+        clk.image_of(torch.zeros(4, 5, 6, dtype=torch.uint16))
+    assert e.value.status == Lm.BAD_ARG and "pinned" in str(e.value)
