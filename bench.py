@@ -611,7 +611,7 @@ def cpu_baseline(a_np, mask_np):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--full-sample", action="store_true", help=argparse.SUPPRESS)
@@ -714,9 +714,11 @@ def main():
     total_ms, value = replicas_value(total_ms, V * len(spec), args.steps, ws, device=dev)
     per = {}
     for name, kind, kernel, params, srcn, ddt, bpv in spec:
-        ms = statistics.mean(a.elapsed_time(b) for a, b in ev[name])
+        runs = [a.elapsed_time(b) for a, b in ev[name]]
+        ms = statistics.mean(runs)
         gbs = V * bpv / (ms * 1e-3) / 1e9
-        per[name] = {"ms": round(ms, 4), "gvox_s": round(V / (ms * 1e-3) / 1e9, 2),
+        per[name] = {"ms": round(ms, 4), "ms_median": round(statistics.median(runs), 4),
+                     "ms_best": round(min(runs), 4), "gvox_s": round(V / (ms * 1e-3) / 1e9, 2),
                      "hbm_frac": round(gbs / peak, 4), "bytes_per_voxel": bpv}
     dom = max(per, key=lambda n: per[n]["ms"])
     dom_gbs = V * per[dom]["bytes_per_voxel"] / (per[dom]["ms"] * 1e-3) / 1e9

@@ -308,8 +308,13 @@ __global__ void __launch_bounds__(256, WRAP ? 2 : 3) k_sobel3d_tile(const S* __r
 
   N A[3][2][2], B[3][2][2], C[3][2][2];
   N ex[2][2], ey[2][2], ez[2][2];
-  uint32_t zflags = 0;
-  auto terms = [&](N (&a)[2][2], N (&b)[2][2], N (&c)[2][2]) {
+  // unsigned pixels: zero pixels among the negative-coefficient taps, per
+  // plane, in the same ring as A, B, C.  Zr: 4-bit counts ZX (column x+1
+  // over 3 rows), ZY (row y+1 over 3 columns), ZZ (the 3x3 block) of the
+  // ring planes; Ec: EX, EY of the newest plane (its taps at dz = +2); one
+  // 16-bit lane per output column ox, one word per output row oy.
+  uint32_t Zr[3][2] = {}, Ec[2] = {};
+  auto terms = [&](N (&a)[2][2], N (&b)[2][2], N (&c)[2][2], uint32_t (&zq)[2]) {
     N v[4][4];  // rows y-1 .. y+2, columns x-1 .. x+2 (clamped by the staging)
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -324,7 +329,28 @@ __global__ void __launch_bounds__(256, WRAP ? 2 : 3) k_sobel3d_tile(const S* __r
       for (int r = 0; r < 4; ++r)
 #pragma unroll
         for (int c = 0; c < 4; ++c) m = min(m, v[r][c]);
-      zflags = (zflags << 1) | (m == 0 ? 1u : 0u);
+      zq[0] = zq[1] = Ec[0] = Ec[1] = 0;
+      if (m == 0) {  // a zero pixel in this thread's 4 x 4 rows of the plane
+        uint32_t zr[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) zr[r][c] = v[r][c] == 0 ? 1u : 0u;
+#pragma unroll
+        for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+          for (int ox = 0; ox < 2; ++ox) {
+            const int rm = oy, rc = oy + 1, rp = oy + 2, sh = 16 * ox;
+            const uint32_t zx = zr[rm][ox + 2] + zr[rc][ox + 2] + zr[rp][ox + 2];
+            const uint32_t zy = zr[rp][ox] + zr[rp][ox + 1] + zr[rp][ox + 2];
+            const uint32_t zz = zr[rm][ox] + zr[rm][ox + 1] + zr[rm][ox + 2] + zr[rc][ox] + zr[rc][ox + 1] +
+                                zr[rc][ox + 2] + zy;
+            const uint32_t e_x = zr[rp][ox + 1] + zr[rm][ox + 2] + zr[rc][ox + 2];
+            const uint32_t e_y = zr[rc][ox] + zr[rc][ox + 1] + zr[rc][ox + 2];
+            zq[oy] |= (zx | (zy << 4) | (zz << 8)) << sh;
+            Ec[oy] |= (e_x | (e_y << 4)) << sh;
+          }
+      }
     }
     N sx[4][2], dx[4][2];
 #pragma unroll
@@ -351,8 +377,9 @@ __global__ void __launch_bounds__(256, WRAP ? 2 : 3) k_sobel3d_tile(const S* __r
   auto step = [&](int zo, auto i0c, auto i1c, auto i2c) {
     constexpr int i0 = decltype(i0c)::value, i1 = decltype(i1c)::value, i2 = decltype(i2c)::value;
     N a[2][2], b[2][2], c[2][2];
+    uint32_t zq[2];
     next_plane();  // plane zo + 2
-    terms(a, b, c);
+    terms(a, b, c, zq);
     float res[2][2];
 #pragma unroll
     for (int oy = 0; oy < 2; ++oy)
@@ -363,10 +390,15 @@ __global__ void __launch_bounds__(256, WRAP ? 2 : 3) k_sobel3d_tile(const S* __r
         const N szv = C[i0][oy][ox] - C[i2][oy][ox] + ez[oy][ox];
         float fx = exact_float(sxv), fy = exact_float(syv), fz = exact_float(szv);
         if constexpr (WRAP) {
+          // K = 12, 12, 9 taps minus the zero pixels among them (planes
+          // zo-1 .. zo+1 from the ring, the dz = +2 taps from Ec)
           float kx = 12.f, ky = 12.f, kz = 9.f;
-          if ((zflags & 0xFu) && act) {  // a zero pixel in planes zo-1 .. zo+2: count exactly
-            const float3 k = wrap_counts<S>(src, W, H, D, x + ox, y + oy, zo);
-            kx = k.x, ky = k.y, kz = k.z;
+          if (Zr[i0][oy] | Zr[i1][oy] | Zr[i2][oy] | Ec[oy]) {
+            const int sh = 16 * ox;
+            const uint32_t sum = Zr[i0][oy] + Zr[i1][oy] + Zr[i2][oy];  // fields <= 9: no carry between them
+            kx = exact_float(12 - (int)(((sum >> sh) & 0xFu) + ((Ec[oy] >> sh) & 0xFu)));
+            ky = exact_float(12 - (int)(((sum >> (sh + 4)) & 0xFu) + ((Ec[oy] >> (sh + 4)) & 0xFu)));
+            kz = exact_float(9 - (int)((Zr[i2][oy] >> (sh + 8)) & 0xFu));
           }
           fx = fmaf(kx, 4294967296.0f, fx);
           fy = fmaf(ky, 4294967296.0f, fy);
@@ -383,18 +415,20 @@ __global__ void __launch_bounds__(256, WRAP ? 2 : 3) k_sobel3d_tile(const S* __r
       }
     }
 #pragma unroll
-    for (int oy = 0; oy < 2; ++oy)
+    for (int oy = 0; oy < 2; ++oy) {
+      Zr[i0][oy] = zq[oy];
 #pragma unroll
       for (int ox = 0; ox < 2; ++ox) A[i0][oy][ox] = a[oy][ox], B[i0][oy][ox] = b[oy][ox], C[i0][oy][ox] = c[oy][ox];
+    }
   };
 
   fetch(z0 - 1);
   next_plane();
-  terms(A[0], B[0], C[0]);
+  terms(A[0], B[0], C[0], Zr[0]);
   next_plane();
-  terms(A[1], B[1], C[1]);
+  terms(A[1], B[1], C[1], Zr[1]);
   next_plane();
-  terms(A[2], B[2], C[2]);
+  terms(A[2], B[2], C[2], Zr[2]);
   using I0 = std::integral_constant<int, 0>;
   using I1 = std::integral_constant<int, 1>;
   using I2 = std::integral_constant<int, 2>;

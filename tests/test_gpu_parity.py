@@ -141,6 +141,25 @@ def test_sobel_fast_path_within_fp64_tolerance(clk, oracle, kernel):
                 assert got16.tobytes() == oracle.execute(kernel, a, np.uint16).tobytes()
 
 
+def test_sobel3d_unsigned_wrap_counts_with_zero_pixels(clk, oracle):
+    # unsigned pixels: every negative-coefficient tap with a nonzero pixel
+    # adds 2^32; zero pixels (masks, sparse stacks, zero borders) change the
+    # counts per output, and a wrong count moves a result by ~8%
+    rng = np.random.default_rng(6)
+    for shp in ((21, 37, 64), (9, 50, 128), (5, 33, 70)):
+        for sdt in (np.uint16, np.uint8):
+            for density in (0.05, 0.5, 0.95):
+                a = random_image(rng, shp, sdt, binary=True, density=density)
+                got = run_execute(clk, "sobel_3d", a, np.float32, {})
+                val, scale = oracle.fp64("sobel_3d", a)
+                assert_fp64_close(got, val, scale, f"sobel_3d {shp} {np.dtype(sdt)} density {density}")
+            b = np.zeros(shp, sdt)  # a zero border around nonzero content
+            b[1:-1, 2:-2, 3:-3] = random_image(rng, (shp[0] - 2, shp[1] - 4, shp[2] - 6), sdt)
+            got = run_execute(clk, "sobel_3d", b, np.float32, {})
+            val, scale = oracle.fp64("sobel_3d", b)
+            assert_fp64_close(got, val, scale, f"sobel_3d {shp} {np.dtype(sdt)} zero border")
+
+
 def test_partial_global_range_writes_only_that_box(clk, oracle):
     rng = np.random.default_rng(5)
     a = random_image(rng, (6, 10, 12), np.uint16)

@@ -83,3 +83,18 @@ def test_2d_and_config_shapes(clk, oracle):
         assert np.array_equal(run(clk, kernel, a, np.uint16, (11, 11, 5), (5, 5, 2)), want), kernel
     val, scale = oracle.fp64("gaussian_blur_separable_3d", a, (19, 19, 11), (3.0, 3.0, 1.5))
     assert close(run(clk, "gaussian_blur_separable_3d", a, np.float32, (19, 19, 11), (3.0, 3.0, 1.5)), val, scale)
+
+
+def test_ragged_tile_grid(clk, oracle):
+    # 15 x 17 tiles whose last column and row are partial (904 = 14 x 64 + 8,
+    # 520 = 16 x 32 + 8), aligned rows (vector staging), 48 planes
+    rng = np.random.default_rng(34)
+    for dt in (np.uint16, np.uint8):
+        a = random_image(rng, (48, 520, 904), dt)
+        for kernel in ("minimum_separable_3d", "maximum_separable_3d", "mean_separable_3d"):
+            want = oracle.separable(kernel, a, dt, (11, 11, 5), (5, 5, 2))
+            assert np.array_equal(run(clk, kernel, a, dt, (11, 11, 5), (5, 5, 2)), want), (kernel, np.dtype(dt))
+    a = random_image(rng, (48, 520, 904), np.uint16)
+    for N, s in (((19, 19, 11), (3.0, 3.0, 1.5)), ((7, 7, 5), (1.0, 1.0, 0.6))):
+        val, scale = oracle.fp64("gaussian_blur_separable_3d", a, N, s)
+        assert close(run(clk, "gaussian_blur_separable_3d", a, np.float32, N, s), val, scale), N
