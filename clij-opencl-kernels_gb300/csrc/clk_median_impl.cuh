@@ -132,16 +132,24 @@ template <class V, int N, int M> __device__ __forceinline__ void pick(const V (&
   for (int k = 0; k < M; ++k) o[k] = w[idx[k]];
 }
 
-// Sorted 9 of the 3x3 block of plane (rows y-1..y+1, columns x-1..x+1) for
-// both lanes, plus optionally the extra values the sphere needs.
+// The 3x3 block of plane (rows y-1..y+1, columns x-1..x+1) for both lanes,
+// unsorted (load9), and sorted (sort9 of those values; block9 = both).
 template <class T, bool ODD, class V>
-__device__ __forceinline__ void block9(const T* plane, int x, int y, int W, int H, V (&p)[9]) {
-  V w[9];
+__device__ __forceinline__ void load9(const T* plane, int x, int y, int W, int H, V (&w)[9]) {
 #pragma unroll
   for (int dy = -1; dy <= 1; ++dy) {
     const T* row = plane + (int64_t)clampi(y + dy, H - 1) * W;
     row_cols<T, ODD>(row, x, W, w[dy + 1], w[dy + 4], w[dy + 7]);
   }
+}
+template <class V> __device__ __forceinline__ void sort9(V (&w)[9], V (&p)[9]);
+template <class T, bool ODD, class V>
+__device__ __forceinline__ void block9(const T* plane, int x, int y, int W, int H, V (&p)[9]) {
+  V w[9];
+  load9<T, ODD>(plane, x, y, W, H, w);
+  sort9(w, p);
+}
+template <class V> __device__ __forceinline__ void sort9(V (&w)[9], V (&p)[9]) {
   {
     V t[3] = {w[0], w[1], w[2]};
     net_sort3_raw(t);
@@ -294,7 +302,18 @@ __device__ __forceinline__ void sphere33_pair_tile(const T* __restrict__ src, T*
   block9<T, ODD>(pl(z0), x, y, W, H, b0);
   block9<T, ODD>(pl(z0 + 1), x, y, W, H, b1);
   block9<T, ODD>(pl(z0 + 2), x, y, W, H, b2);
+  V s0[6];
+  singles(z0, s0);
   for (int zo = z0; zo < z1; zo += 2) {
+    // the next pair's blocks (planes zo+3, zo+4) are loaded before this
+    // pair's networks run and sorted after them: their latency hides
+    // behind the merge and the two finals
+    const bool more = zo + 2 < z1;
+    V r3[9], r4[9];
+    if (more) {
+      load9<T, ODD>(pl(zo + 3), x, y, W, H, r3);
+      load9<T, ODD>(pl(zo + 4), x, y, W, H, r4);
+    }
     V m[16];
     {
       V w[18];
@@ -303,18 +322,16 @@ __device__ __forceinline__ void sphere33_pair_tile(const T* __restrict__ src, T*
       net_merge99_r1_16_raw(w);
       pick(w, net_merge99_r1_16_out, m);
     }
-    V s[6];
-    singles(zo, s);
-    store_pair<T, ODD>(dst + (int64_t)zo * plane + (int64_t)y * W, x, W, final(m, bm1, s));
-    if (zo + 1 < z1) {
-      singles(zo + 1, s);
-      store_pair<T, ODD>(dst + (int64_t)(zo + 1) * plane + (int64_t)y * W, x, W, final(m, b2, s));
-    }
-    if (zo + 2 < z1) {
+    V s1[6];
+    if (zo + 1 < z1) singles(zo + 1, s1);
+    store_pair<T, ODD>(dst + (int64_t)zo * plane + (int64_t)y * W, x, W, final(m, bm1, s0));
+    if (more) singles(zo + 2, s0);
+    if (zo + 1 < z1) store_pair<T, ODD>(dst + (int64_t)(zo + 1) * plane + (int64_t)y * W, x, W, final(m, b2, s1));
+    if (more) {
 #pragma unroll
       for (int k = 0; k < 9; ++k) bm1[k] = b1[k], b0[k] = b2[k];
-      block9<T, ODD>(pl(zo + 3), x, y, W, H, b1);
-      block9<T, ODD>(pl(zo + 4), x, y, W, H, b2);
+      sort9(r3, b1);
+      sort9(r4, b2);
     }
   }
 }
