@@ -201,13 +201,21 @@ __device__ __forceinline__ void box27_tile(const T* __restrict__ src, T* __restr
   if (x >= W || y >= H) return;
   const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
   const int64_t plane = (int64_t)W * H;
-  V pm1[9], p0[9];
+  V pm1[9], p0[9], r1[9], r2[9];
   block9<T, ODD>(src + (int64_t)clampi(z0 - 1, D - 1) * plane, x, y, W, H, pm1);
   block9<T, ODD>(src + (int64_t)z0 * plane, x, y, W, H, p0);
+  load9<T, ODD>(src + (int64_t)clampi(z0 + 1, D - 1) * plane, x, y, W, H, r1);
+  load9<T, ODD>(src + (int64_t)clampi(z0 + 2, D - 1) * plane, x, y, W, H, r2);
   for (int zo = z0; zo < z1; zo += 2) {
+    // planes zo+1, zo+2 were loaded one pair ahead; the loads of zo+3,
+    // zo+4 go out before this pair's networks
     V p1[9], p2[9], m[10];
-    block9<T, ODD>(src + (int64_t)clampi(zo + 1, D - 1) * plane, x, y, W, H, p1);
-    block9<T, ODD>(src + (int64_t)clampi(zo + 2, D - 1) * plane, x, y, W, H, p2);
+    sort9(r1, p1);
+    sort9(r2, p2);
+    if (zo + 2 < z1) {
+      load9<T, ODD>(src + (int64_t)clampi(zo + 3, D - 1) * plane, x, y, W, H, r1);
+      load9<T, ODD>(src + (int64_t)clampi(zo + 4, D - 1) * plane, x, y, W, H, r2);
+    }
     merge_mid(p0, p1, m);
     store_pair<T, ODD>(dst + (int64_t)zo * plane + (int64_t)y * W, x, W, final27(m, pm1));
     if (zo + 1 < z1) store_pair<T, ODD>(dst + (int64_t)(zo + 1) * plane + (int64_t)y * W, x, W, final27(m, p2));
