@@ -97,8 +97,10 @@ __global__ void __launch_bounds__(MT)
     k_morph_bytes(const S* __restrict__ src, D* __restrict__ dst, int W, int H, int Dz, int zchunk) {
   using G = Geo<ITER>;
   constexpr bool PLANAR = ITER == 0;
-  __shared__ uint4 in[3][G::IY * G::IX];
-  __shared__ uint4 mid[ITER == 2 ? 3 : 1][ITER == 2 ? G::SY * G::SX : 1];
+  // ITER 0: two input planes; ITER 1: a ring of four; ITER 2: rings of four
+  // input and four intermediate planes in dynamic shared memory (49 KiB)
+  __shared__ uint4 in[ITER == 2 ? 1 : 4][ITER == 2 ? 1 : G::IY * G::IX];
+  extern __shared__ uint4 dsm[];
   const int nxc = W / 16;
   const int xc0 = blockIdx.x * MX, y0 = blockIdx.y * MY;
   const int z0 = blockIdx.z * zchunk, z1 = min(Dz, z0 + zchunk);
@@ -127,14 +129,15 @@ __global__ void __launch_bounds__(MT)
       }
     }
   };
-  auto load_plane = [&](int zv, int slot) {
+  auto stage = [&](int zv, uint4* to) {
 #pragma unroll
     for (int k = 0; k < PERM; ++k) {
       const int i = tid + k * MT;
-      if (i < NS) in[slot][i] = nzmask(pf[k]);
+      if (i < NS) to[i] = nzmask(pf[k]);
     }
     if (zv + 1 <= last_in) fetch(zv + 1);
   };
+  auto load_plane = [&](int zv, int slot) { stage(zv, in[slot]); };
   fetch(PLANAR ? z0 : z0 - ITER);
   auto store = [&](int zo, int r, int q, uint4 m) {
     const int gy = y0 + r, gq = xc0 + q;
@@ -155,87 +158,65 @@ __global__ void __launch_bounds__(MT)
       store(zo, r, q, step<ERODE, SPHERE>(in[b], in[b], in[b], G::IX, r, q, gq == 0, gq == nxc - 1));
     }
   } else if constexpr (ITER == 1) {
-    load_plane(z0 - 1, 0);
-    load_plane(z0, 1);
-    for (int zo = z0; zo < z1; ++zo) {
-      load_plane(zo + 1, (zo + 2 - z0) % 3);
-      __syncthreads();
-      const uint4* A = in[(zo - z0) % 3];
-      const uint4* B = in[(zo + 1 - z0) % 3];
-      const uint4* C = in[(zo + 2 - z0) % 3];
-      const int r = tid / MX, q = tid % MX;
-      const int gq = xc0 + q;
-      store(zo, r, q, step<ERODE, SPHERE>(A, B, C, G::IX, r, q, gq == 0, gq == nxc - 1));
+    // Phase j stages input j+2 and filters output plane j from inputs
+    // j-1 .. j+1 (staged in earlier phases): a ring of four input planes
+    // (plane p in slot p & 3) and one barrier per plane.
+    for (int j = z0 - 3; j < z1; ++j) {
+      if (j + 2 <= last_in) stage(j + 2, in[(j + 2) & 3]);
+      if (j >= z0) {
+        const int r = tid / MX, q = tid % MX;
+        const int gq = xc0 + q;
+        store(j, r, q, step<ERODE, SPHERE>(in[(j - 1) & 3], in[j & 3], in[(j + 1) & 3], G::IX, r, q, gq == 0,
+                                           gq == nxc - 1));
+      }
       __syncthreads();
     }
   } else {
-    // Intermediate plane p (virtual index) is the first step evaluated at
-    // clamp(p): rows/planes outside the image are copies of the border
-    // row/plane.  Region rows r = 0..R1Y-1 <-> global rows y0-1+r, chunks
-    // q <-> xc0-1+q; stored densely with pitch SX (= R1X).
-    auto compute_mid = [&](int p, int sa, int sb, int sc) {
-      uint4* M = mid[(p - (z0 - 1)) % 3];
-      for (int i = tid; i < G::R1Y * G::R1X; i += MT) {
-        const int r = i / G::R1X, q = i - r * G::R1X;
-        const int gq = clampi(xc0 - 1 + q, nxc - 1);
-        M[r * G::SX + q] = step<ERODE, SPHERE>(in[sa], in[sb], in[sc], G::IX, r, q, gq == 0, gq == nxc - 1);
-      }
-      __syncthreads();
-      // rows of the region above / below the image repeat the border row
-      for (int i = tid; i < G::R1Y * G::R1X; i += MT) {
-        const int r = i / G::R1X, q = i - r * G::R1X;
-        const int gy = y0 - 1 + r;
-        if (gy < 0 || gy >= H) {
-          const int rc = clampi(gy, H - 1) - (y0 - 1);
-          M[r * G::SX + q] = M[rc * G::SX + q];
+    // Phase j stages input j+4, computes the intermediate (first step) at
+    // plane j+2 from inputs j+1 .. j+3, and filters output plane j from the
+    // intermediates j-1 .. j+1: rings of four input and four intermediate
+    // planes (plane p in slot p & 3), one barrier per plane.
+    //
+    // The intermediate at a virtual position is the one at the clamped
+    // position: rows above / below the image evaluate the first step at the
+    // clamped row; plane -1 (Dz) is a copy of plane 0 (Dz - 1), made in the
+    // phase after that plane is computed.  Intermediate region rows
+    // r = 0..R1Y-1 <-> global rows y0-1+r, chunks q <-> xc0-1+q.
+    constexpr int MS = G::SY * G::SX;
+    auto ip = [&](int p) { return dsm + (p & 3) * NS; };
+    auto mp = [&](int p) { return dsm + 4 * NS + (p & 3) * MS; };
+    for (int j = z0 - 6; j < z1; ++j) {
+      if (j + 4 <= last_in) stage(j + 4, ip(j + 4));
+      const int pm = j + 2;
+      if (pm >= z0 - 1 && pm <= z1) {
+        if (pm >= 0 && pm < Dz) {
+          uint4* M = mp(pm);
+          for (int i = tid; i < G::R1Y * G::R1X; i += MT) {
+            const int r = i / G::R1X, q = i - r * G::R1X;
+            const int gy = y0 - 1 + r;
+            const int rr = r + (clampi(gy, H - 1) - gy);
+            const int gq = clampi(xc0 - 1 + q, nxc - 1);
+            M[r * G::SX + q] = step<ERODE, SPHERE>(ip(pm - 1), ip(pm), ip(pm + 1), G::IX, rr, q, gq == 0,
+                                                   gq == nxc - 1);
+          }
+        } else if (pm >= Dz) {  // plane Dz: copy of Dz - 1 (computed in the previous phase)
+          const uint4* Mf = mp(Dz - 1);
+          uint4* Mt = mp(pm);
+          for (int i = tid; i < MS; i += MT) Mt[i] = Mf[i];
         }
       }
-    };
-    // input plane zv lives in in[(zv - (z0 - 2)) % 3]
-    auto islot = [&](int zv) { return ((zv - (z0 - 2)) % 3 + 3) % 3; };
-    auto mslot = [&](int p) { return ((p - (z0 - 1)) % 3 + 3) % 3; };
-    // the intermediate at virtual plane p is the one at clamp(p): compute
-    // real planes from their own (clamped) inputs, copy for virtual ones
-    auto mid_for = [&](int p) {
-      const int pc = clampi(p, Dz - 1);
-      if (pc != p) return;  // filled by copy below
-      compute_mid(p, islot(p - 1), islot(p), islot(p + 1));
-    };
-    auto copy_mid = [&](int to, int from) {
-      uint4* Mt = mid[mslot(to)];
-      const uint4* Mf = mid[mslot(from)];
-      for (int i = tid; i < G::SY * G::SX; i += MT) Mt[i] = Mf[i];
-    };
-    // prologue: inputs z0-2 .. z0+1, intermediates z0-1 .. z0
-    load_plane(z0 - 2, islot(z0 - 2));
-    load_plane(z0 - 1, islot(z0 - 1));
-    load_plane(z0, islot(z0));
-    for (int zo = z0; zo < z1; ++zo) {
-      if (zo == z0) {
-        // intermediate z0-1 needs inputs z0-2..z0; intermediate z0 needs z0+1
-        __syncthreads();
-        if (z0 - 1 >= 0) mid_for(z0 - 1);
-        __syncthreads();
-        load_plane(z0 + 1, islot(z0 + 1));
-        __syncthreads();
-        mid_for(z0);
-        __syncthreads();
-        if (z0 - 1 < 0) copy_mid(z0 - 1, 0);
+      if (j == -1 && z0 == 0) {  // plane -1: copy of plane 0 (computed in the previous phase)
+        const uint4* Mf = mp(0);
+        uint4* Mt = mp(-1);
+        for (int i = tid; i < MS; i += MT) Mt[i] = Mf[i];
       }
-      // intermediate zo+1 needs input zo+2 (overwrites input zo-1's slot)
+      if (j >= z0) {
+        const int r = tid / MX, q = tid % MX;
+        const int gq = xc0 + q;
+        // output tile (r, q) sits at (r+1, q+1) of the intermediate region
+        store(j, r, q, step<ERODE, SPHERE>(mp(j - 1), mp(j), mp(j + 1), G::SX, r, q, gq == 0, gq == nxc - 1));
+      }
       __syncthreads();
-      load_plane(zo + 2, islot(zo + 2));
-      __syncthreads();
-      if (zo + 1 <= Dz - 1) mid_for(zo + 1);
-      else copy_mid(zo + 1, Dz - 1);
-      __syncthreads();
-      const int r = tid / MX, q = tid % MX;
-      const int gq = xc0 + q;
-      // output tile (r, q) sits at (r+1, q+1) of the intermediate region
-      const uint4* A = mid[mslot(zo - 1)];
-      const uint4* B = mid[mslot(zo)];
-      const uint4* C = mid[mslot(zo + 1)];
-      store(zo, r, q, step<ERODE, SPHERE>(A, B, C, G::SX, r, q, gq == 0, gq == nxc - 1));
     }
   }
 }
@@ -251,8 +232,16 @@ clk_status launch_morph(const Image& dst, const Image& src, cudaStream_t st) {
   while ((int64_t)tx * ty * chunks < 8LL * sms && src.d / (chunks * 2) >= 16) chunks *= 2;
   const int zchunk = (src.d + chunks - 1) / chunks;
   dim3 grid(tx, ty, (src.d + zchunk - 1) / zchunk);
-  k_morph_bytes<S, D, ERODE, SPHERE, ITER><<<grid, MT, 0, st>>>((const S*)src.ptr, (D*)dst.ptr, src.w, src.h,
-                                                                  src.d, zchunk);
+  using G = Geo<ITER>;
+  const size_t smem = ITER == 2 ? 4 * sizeof(uint4) * (G::IY * G::IX + G::SY * G::SX) : 0;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_morph_bytes<S, D, ERODE, SPHERE, ITER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return CLK_UNSUPPORTED_DTYPE;
+  }
+  k_morph_bytes<S, D, ERODE, SPHERE, ITER><<<grid, MT, smem, st>>>((const S*)src.ptr, (D*)dst.ptr, src.w, src.h,
+                                                                     src.d, zchunk);
   count_launch();
   return check_launch("morphology (byte tiles)");
 }

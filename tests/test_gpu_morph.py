@@ -49,7 +49,10 @@ def oracle_iter(oracle, kernel, a, ddt, iterations):
 @pytest.mark.parametrize("density", [0.5, 0.93])
 def test_byte_tiles_match_oracle(clk, oracle, kernel, density):
     rng = np.random.default_rng(17)
-    for shp in ((37, 70, 160), (5, 33, 48), (1, 9, 16), (40, 1, 32), (3, 64, 512)):
+    # also: two-plane stacks, and deep thin stacks whose z-chunks (CTAs)
+    # start and end inside the stack
+    for shp in ((37, 70, 160), (5, 33, 48), (1, 9, 16), (40, 1, 32), (3, 64, 512), (2, 40, 64), (70, 40, 32),
+                (100, 20, 16)):
         a = random_image(rng, shp, np.uint8, binary=True, density=density)
         for it in (1, 2, 3, 4):
             got = run(clk, kernel, a, np.uint8, it)
