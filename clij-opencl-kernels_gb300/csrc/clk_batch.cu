@@ -23,6 +23,7 @@
 #include <mutex>
 #include <sstream>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "clk_batch.cuh"
@@ -36,6 +37,16 @@ const void* batch_sep_kernel(int op, int R, int dt) {
     case SEP_MEAN: return batch_sep_kernel_op<SEP_MEAN>(R, dt);
     case SEP_MIN: return batch_sep_kernel_op<SEP_MIN>(R, dt);
     case SEP_MAX: return batch_sep_kernel_op<SEP_MAX>(R, dt);
+  }
+  return nullptr;
+}
+
+const void* batch_sep2_kernel(int op, int R, int dt) {
+  switch (op) {
+    case SEP_GAUSS: return batch_sep2_kernel_op<SEP_GAUSS>(R, dt);
+    case SEP_MEAN: return batch_sep2_kernel_op<SEP_MEAN>(R, dt);
+    case SEP_MIN: return batch_sep2_kernel_op<SEP_MIN>(R, dt);
+    case SEP_MAX: return batch_sep2_kernel_op<SEP_MAX>(R, dt);
   }
   return nullptr;
 }
@@ -60,10 +71,16 @@ bool batch_radius(int R) {
 }
 
 // shared memory of a sep2 tile body (host side of sep2::Geo)
-template <class T, int OP, int R> size_t sep2_smem_t(int cz) { return sep2::Geo<T, S2Op<OP>::v, R>::smem(cz); }
+template <class T, int OP, int R> size_t sep2_smem_t(int cz) { return sep2::Geo<T, S2OpT<OP, T>::v, R>::smem(cz); }
 template <int OP, int R> size_t sep2_smem_r(int dt, int cz) {
-  if constexpr (OP == SEP_GAUSS) {  // the register-window Gaussian writes float
-    return dt == CLK_F32 ? sep2_smem_t<float, OP, R>(cz) : 0;
+  if constexpr (OP == SEP_GAUSS) {  // float: the FMA Gaussian; 8/16-bit: the exact-order one
+    switch (dt) {
+      case CLK_F32: return sep2_smem_t<float, OP, R>(cz);
+      case CLK_U8: return sep2_smem_t<uint8_t, OP, R>(cz);
+      case CLK_U16: return sep2_smem_t<uint16_t, OP, R>(cz);
+      case CLK_I16: return sep2_smem_t<int16_t, OP, R>(cz);
+    }
+    return 0;
   } else {  // min/max/mean: 8/16-bit pixels
     switch (dt) {
       case CLK_U8: return sep2_smem_t<uint8_t, OP, R>(cz);
@@ -305,12 +322,19 @@ ImgStep plan_sep(clk_batch* b, int s, int i, SepDesc* d) {
     const int R = cx;
     const bool s2_int = ints && opn != SEP_GAUSS && R <= 8;
     const bool s2_gauss = fast && R <= 12;
-    if (s2_int || s2_gauss) {
+    const bool s2_gx = ints && opn == SEP_GAUSS && R <= 8 && in.dt == out.dt;  // exact order, as the plain path
+    if (s2_int || s2_gauss || s2_gx) {
       if (!batch_radius(R) || sep2_smem(opn, R, in.dt, cz) > 220 * 1024) return h;  // plain call keeps parity
       d->algo = A_SEP2;
       d->p2.cz = cz;
       d->p2.mx = sep2::recip32(2 * R + 1);
       d->p2.mz = sep2::recip32(2 * cz + 1);
+      if (s2_gx) {
+        for (int v = 0; v <= 2 * R; ++v) d->p2.hx[v] = ft.h[0][v], d->p2.hy[v] = ft.h[1][v];
+        for (int v = 0; v <= 2 * cz; ++v) d->p2.hz[v] = ft.h[2][v];
+        for (int a = 0; a < 3; ++a) d->p2.hs[a] = ft.hsum[a];
+        d->p2.rte = plan.pol.rte ? 1 : 0;
+      }
       if (s2_gauss) {
         for (int a = 0; a < 3; ++a) {
           const int c = ft.c[a];
@@ -648,15 +672,17 @@ clk_status clk_batch_create(const clk_op* ops, int32_t nops, const clk_image* sr
     const bool med = b->names[s] == "median_box" || b->names[s] == "median_sphere";
     if (b->ops[s].kind == CLK_OP_SEPARABLE && sop >= 0) {
       std::vector<SepDesc> hd(nimages);
-      std::map<std::pair<int, int>, int> gi;  // (R, dt) -> group
+      std::map<std::tuple<int, int, bool>, int> gi;  // (R, dt, register-window body) -> group
       for (int i = 0; i < nimages; ++i) {
         b->how[s][i] = plan_sep(b, s, i, &hd[i]);
         if (!b->how[s][i].algo) continue;
-        const auto key = std::make_pair(b->how[s][i].R, b->src[i].dt);
+        const bool s2 = b->how[s][i].algo == A_SEP2;
+        const auto key = std::make_tuple(b->how[s][i].R, b->src[i].dt, s2);
         if (!gi.count(key)) {
           Group g;
-          g.kernel = batch_sep_kernel(sop, key.first, key.second);
-          g.dt = key.second;
+          g.kernel = s2 ? batch_sep2_kernel(sop, std::get<0>(key), std::get<1>(key))
+                        : batch_sep_kernel(sop, std::get<0>(key), std::get<1>(key));
+          g.dt = std::get<1>(key);
           if (!g.kernel) {
             b->how[s][i].algo = 0;
             continue;

@@ -46,6 +46,10 @@ template <> struct S2Op<SEP_MIN> { static constexpr int v = sep2::MIN; };
 template <> struct S2Op<SEP_MAX> { static constexpr int v = sep2::MAX; };
 template <> struct S2Op<SEP_MEAN> { static constexpr int v = sep2::MEAN; };
 template <> struct S2Op<SEP_GAUSS> { static constexpr int v = sep2::GAUSS; };
+// ... for pixel type T: the Gaussian to 8/16-bit pixels is the exact-order one
+template <int OP, class T> struct S2OpT {
+  static constexpr int v = (OP == SEP_GAUSS && sizeof(T) < 4) ? (int)sep2::GAUSSX : S2Op<OP>::v;
+};
 
 constexpr int kmax_for(int R) { return R == 0 ? 63 : (2 * R + 1 <= 12 ? 12 : 24); }
 
@@ -55,18 +59,6 @@ __device__ __forceinline__ void sep_item_t(const SepDesc& d, const WorkItem& it,
   constexpr int KMAX = kmax_for(R);
   const T* s = static_cast<const T*>(d.src);
   T* o = static_cast<T*>(d.dst);
-  if constexpr (R >= 1 && sizeof(T) < 4 && OP != SEP_GAUSS) {
-    if (d.algo == A_SEP2) {
-      sep2::sep2_tile<T, T, S2Op<OP>::v, R>(s, o, d.W, d.H, d.D, d.zchunk, d.p2, it.bx, it.by, it.bz, smem);
-      return;
-    }
-  }
-  if constexpr (R >= 1 && sizeof(T) == 4 && OP == SEP_GAUSS) {
-    if (d.algo == A_SEP2) {
-      sep2::sep2_tile<T, T, sep2::GAUSS, R>(s, o, d.W, d.H, d.D, d.zchunk, d.p2, it.bx, it.by, it.bz, smem);
-      return;
-    }
-  }
   if constexpr (sizeof(T) == 4 && OP == SEP_GAUSS) {
     if (d.algo == A_FUSED_FAST) {
       fused::fused_tile<T, T, OP, true, KMAX>(s, o, d.W, d.H, d.D, d.zchunk, d.ft, d.rte, it.bx, it.by, it.bz, smem);
@@ -76,8 +68,22 @@ __device__ __forceinline__ void sep_item_t(const SepDesc& d, const WorkItem& it,
   fused::fused_tile<T, T, OP, false, KMAX>(s, o, d.W, d.H, d.D, d.zchunk, d.ft, d.rte, it.bx, it.by, it.bz, smem);
 }
 
-// One persistent kernel per step and pixel type (a kernel's register
-// budget is that of its largest branch, so pixel types are not mixed).
+// One persistent kernel per step, pixel type and body: the register-window
+// tiles (A_SEP2) and the generic fused tiles run as separate kernels, since
+// a kernel's register budget is that of its largest branch.
+template <int OP, int R, class T>
+__global__ void __launch_bounds__(256, 2) k_batch_sep2(const WorkItem* __restrict__ items, int n,
+                                                       const SepDesc* __restrict__ descs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const WorkItem it = items[i];
+    const SepDesc& d = descs[it.img];
+    sep2::sep2_tile<T, T, S2OpT<OP, T>::v, R>(static_cast<const T*>(d.src), static_cast<T*>(d.dst), d.W, d.H, d.D,
+                                               d.zchunk, d.p2, it.bx, it.by, it.bz, smem);
+    __syncthreads();  // the next item reuses shared memory
+  }
+}
+// The generic fused tiles of a step and pixel type.
 template <int OP, int R, class T>
 __global__ void __launch_bounds__(256) k_batch_sep(const WorkItem* __restrict__ items, int n,
                                                    const SepDesc* __restrict__ descs) {
@@ -116,6 +122,9 @@ __global__ void __launch_bounds__(256) k_batch_median(const WorkItem* __restrict
 // variant.  nullptr if not instantiated.
 const void* batch_sep_kernel(int op, int R, int dt);
 template <int OP> const void* batch_sep_kernel_op(int R, int dt);  // one file per OP
+// the register-window kernel for (op, R >= 1, pixel type); nullptr if none
+const void* batch_sep2_kernel(int op, int R, int dt);
+template <int OP> const void* batch_sep2_kernel_op(int R, int dt);
 const void* batch_median_kernel(int dt);
 constexpr int kBatchRadii[] = {2, 3, 4, 5, 6};  // instantiated XY radii besides 0
 

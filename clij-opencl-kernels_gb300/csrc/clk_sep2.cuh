@@ -36,6 +36,11 @@ struct Params {
   float wz[kMaxCz + 1];  //         ... of Z
   uint32_t mx, mz;     // mean: reciprocal multipliers (recip32) for N = 2R+1 and 2cz+1
   int cz;
+  // Gaussian to integer pixels (exact order): the reference's taps h[v],
+  // v = -c..c, of each pass and their float sums
+  float hx[17], hy[17], hz[2 * kMaxCz + 1];
+  float hs[3];
+  int rte;
 };
 
 // ---------------------------------------------------------------- lanes
@@ -109,11 +114,46 @@ template <class T> __device__ __forceinline__ uint32_t lane16(T v) {
 }
 template <class T> __device__ __forceinline__ T from_lane16(uint32_t l) { return (T)(int16_t)(uint16_t)l; }
 
+// The two 16-bit lanes of w (signed or not) as an f32x2 pair, exactly: the
+// float 2^23 + v (+ 2^15 for signed lanes) built by a byte permute, minus
+// the same constant.
+template <bool SGN> __device__ __forceinline__ uint64_t f2_of_lanes(uint32_t w) {
+  constexpr uint32_t K = 0x4B000000u;
+  uint32_t a = __byte_perm(w, K, 0x7410), b = __byte_perm(w, K, 0x7432);
+  if constexpr (SGN) a ^= 0x8000u, b ^= 0x8000u;
+  constexpr float off = 8388608.0f + (SGN ? 32768.0f : 0.0f);
+  return f2_add(f2_pack(__uint_as_float(a), __uint_as_float(b)), f2_bcast(-off));
+}
+
+// One exact-order Gaussian output pair: sum of h[v] * win[v], v = 0..N-1, in
+// that order with separately rounded products and sums (the reference's
+// loop), divided by hsum (IEEE), converted to D; returned as 16-bit lanes.
+// Scalar __fmul_rn / __fadd_rn per lane: a packed mul.rn.f32x2 followed by
+// add.rn.f32x2 gave results that differed from them in the last bit now and
+// then (measured: about 1 in 3000 outputs one unit off after conversion).
+template <class D, int N> __device__ __forceinline__ uint32_t gauss_exact_pair(const uint64_t* win, const float* h,
+                                                                              float hsum, bool rte) {
+  float2 f = f2_unpack(win[0]);
+  f.x = __fmul_rn(h[0], f.x), f.y = __fmul_rn(h[0], f.y);
+#pragma unroll
+  for (int v = 1; v < N; ++v) {
+    const float2 x = f2_unpack(win[v]);
+    f.x = __fadd_rn(f.x, __fmul_rn(h[v], x.x));
+    f.y = __fadd_rn(f.y, __fmul_rn(h[v], x.y));
+  }
+  const D a = convert_sat<D>(__fdiv_rn(f.x, hsum), rte), b = convert_sat<D>(__fdiv_rn(f.y, hsum), rte);
+  return lane16(a) | (lane16(b) << 16);
+}
+
 }  // namespace sep2
 
 clk_status sep2_minmax(bool is_max, int R, const Image& dst, const Image& src, int cz, cudaStream_t st);
 clk_status sep2_mean(int R, const Image& dst, const Image& src, int cz, cudaStream_t st);
 clk_status sep2_gauss(int R, const Image& dst, const Image& src, const float* wx, const float* wy, const float* wz,
                       int cz, cudaStream_t st);
+// Gaussian with integer temporaries and outputs, bit-exact: h[d] are the
+// 2c+1 taps of pass d (v = -c..c), hs[d] their float sums
+clk_status sep2_gauss_exact(int R, const Image& dst, const Image& src, const float* const h[3], const float hs[3],
+                            int cz, bool rte, cudaStream_t st);
 
 }  // namespace clk

@@ -13,7 +13,9 @@ namespace clk {
 namespace sep2 {
 namespace {
 
-enum Op { MIN = 0, MAX = 1, MEAN = 2, GAUSS = 3 };
+// GAUSSX: the Gaussian to 8/16-bit pixels in the reference's arithmetic
+// (taps in order, separately rounded, IEEE division, dst-typed temporaries)
+enum Op { MIN = 0, MAX = 1, MEAN = 2, GAUSS = 3, GAUSSX = 4 };
 
 // temporaries: 16-bit lanes for integer pixels, float for the Gaussian
 template <class S, int OP> struct Temp;
@@ -21,6 +23,7 @@ template <class S> struct Temp<S, MIN> { typedef typename std::conditional<Is16<
 template <class S> struct Temp<S, MAX> { typedef typename std::conditional<Is16<S>::sgn, int16_t, uint16_t>::type T; };
 template <class S> struct Temp<S, MEAN> { typedef typename std::conditional<Is16<S>::sgn, int16_t, uint16_t>::type T; };
 template <class S> struct Temp<S, GAUSS> { typedef float T; };
+template <class S> struct Temp<S, GAUSSX> { typedef typename std::conditional<Is16<S>::sgn, int16_t, uint16_t>::type T; };
 
 template <class S, int OP> __device__ __forceinline__ uint32_t mm(uint32_t a, uint32_t b) {
   if constexpr (Is16<S>::sgn) return OP == MIN ? s16x2_min(a, b) : s16x2_max(a, b);
@@ -374,6 +377,21 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
             *reinterpret_cast<uint32_t*>(o0 + j) = __byte_perm((uint32_t)q0[j], (uint32_t)q0[j + 1], 0x5410);
             *reinterpret_cast<uint32_t*>(o1 + j) = __byte_perm((uint32_t)q1[j], (uint32_t)q1[j + 1], 0x5410);
           }
+        } else if constexpr (OP == GAUSSX) {
+          uint64_t win[G::WIN_X];
+#pragma unroll
+          for (int k = 0; k < G::WIN_X; ++k) {
+            if constexpr (MODE == STAGE_SCALAR) win[k] = f2_pack(tofloat(r0[k]), tofloat(r1[k]));
+            else win[k] = f2_of<S>(w0, w1, XOFF + k);
+          }
+          uint32_t q[SEGX];  // lane 0: row 0, lane 1: row 1
+#pragma unroll
+          for (int j = 0; j < SEGX; ++j) q[j] = gauss_exact_pair<D, 2 * R + 1>(win + j, p.hx, p.hs[0], p.rte);
+#pragma unroll
+          for (int j = 0; j < SEGX; j += 2) {
+            *reinterpret_cast<uint32_t*>(o0 + j) = __byte_perm(q[j], q[j + 1], 0x5410);
+            *reinterpret_cast<uint32_t*>(o1 + j) = __byte_perm(q[j], q[j + 1], 0x7632);
+          }
         } else {
           uint64_t win[G::WIN_X];
 #pragma unroll
@@ -433,6 +451,14 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
           zs0[j] += q0;  // the new plane enters the running z sums
           zs1[j] += q1;
         }
+      } else if constexpr (OP == GAUSSX) {
+        uint64_t win[G::WIN_Y];
+#pragma unroll
+        for (int k = 0; k < G::WIN_Y; ++k)
+          win[k] = f2_of_lanes<Is16<S>::sgn>(*reinterpret_cast<const uint32_t*>(col + k * G::XP));
+#pragma unroll
+        for (int j = 0; j < SEGY; ++j)
+          *reinterpret_cast<uint32_t*>(o + j * TX) = gauss_exact_pair<D, 2 * R + 1>(win + j, p.hy, p.hs[1], p.rte);
       } else {
         uint64_t win[G::WIN_Y];
 #pragma unroll
@@ -459,7 +485,38 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
       // even widths keep every row pair-aligned: one store for both lanes;
       // odd widths store the lanes separately (the second may lie past W)
       const bool pair = (W & 1) == 0;
-      if constexpr (OP == MIN || OP == MAX) {
+      if constexpr (OP == GAUSSX) {
+        // planes zo-cz .. zo+cz in order, from the oldest ring slot on
+        float2 acc[SEGY];
+        int idx = oldest;
+        for (int v = 0; v < NZ; ++v) {
+          const T* c = cells + (size_t)idx * PL;
+          const float hv = p.hz[v];
+#pragma unroll
+          for (int j = 0; j < SEGY; ++j) {
+            const float2 x = f2_unpack(f2_of_lanes<Is16<S>::sgn>(*reinterpret_cast<const uint32_t*>(c + j * TX)));
+            const float mx = __fmul_rn(hv, x.x), my = __fmul_rn(hv, x.y);
+            acc[j] = v == 0 ? make_float2(mx, my) : make_float2(__fadd_rn(acc[j].x, mx), __fadd_rn(acc[j].y, my));
+          }
+          idx = idx + 1 == NZ ? 0 : idx + 1;
+        }
+#pragma unroll
+        for (int j = 0; j < SEGY; ++j) {
+          const float2 f = acc[j];
+          const D a = convert_sat<D>(__fdiv_rn(f.x, p.hs[2]), p.rte), b = convert_sat<D>(__fdiv_rn(f.y, p.hs[2]), p.rte);
+          const int gy = y0 + sy * SEGY + j;
+          D* out = dst + (int64_t)zo * plane + (int64_t)gy * W + gx;
+          if (gy < H && gx < W) {
+            if (pair) {
+              if constexpr (sizeof(D) == 2) *reinterpret_cast<uint32_t*>(out) = lane16(a) | (lane16(b) << 16);
+              else *reinterpret_cast<uint16_t*>(out) = (uint16_t)((uint8_t)a | ((uint32_t)(uint8_t)b << 8));
+            } else {
+              out[0] = a;
+              if (gx + 1 < W) out[1] = b;
+            }
+          }
+        }
+      } else if constexpr (OP == MIN || OP == MAX) {
         uint32_t a[SEGY];
         const T* c = cells + (size_t)oldest * PL;
 #pragma unroll
@@ -601,7 +658,9 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
 
 // CTAs per SM the register budget is sized for (64 / 80 / 128 registers;
 // the vector staging holds fewer prefetch registers than the scalar one)
-template <int OP, int MODE> constexpr int min_ctas() { return OP == GAUSS ? 2 : MODE == STAGE_VEC ? 4 : 3; }
+template <int OP, int MODE> constexpr int min_ctas() {
+  return OP == GAUSS ? 2 : OP == GAUSSX ? (MODE == STAGE_VEC ? 3 : 2) : MODE == STAGE_VEC ? 4 : 3;
+}
 
 template <class S, class D, int OP, int R, int MODE, bool PIPE = false>
 __global__ void __launch_bounds__(NT, min_ctas<OP, MODE>()) k_sep2(const S* __restrict__ src, D* __restrict__ dst, int W,

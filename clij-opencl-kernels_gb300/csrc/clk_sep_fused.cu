@@ -116,6 +116,10 @@ clk_status fused_separable(SepOp op, const Image& dst, const Image& src, const S
       s2 = sep2_minmax(op == SEP_MAX, R, dst, src, cz, st);
     } else if (op == SEP_MEAN && ints) {
       s2 = sep2_mean(R, dst, src, cz, st);
+    } else if (op == SEP_GAUSS && ints) {
+      // integer outputs: the reference's order and rounding, pass by pass
+      const float* h[3] = {ft.h[0], ft.h[1], ft.h[2]};
+      s2 = sep2_gauss_exact(R, dst, src, h, ft.hsum, cz, p.rte, st);
     } else if (fast) {
       // folded taps: w[0] for the centre, w[k] for the pair +-k, all / sum(h)
       float w[3][kFusedMaxR + 1] = {};

@@ -21,12 +21,12 @@ def clk():
     return m
 
 
-def run(clk, kernel, a, ddt, N, s):
+def run(clk, kernel, a, ddt, N, s, defines=None):
     import torch
     from clk.api import torch_dtype
     from oracle.oracle import dtype_code
     d = torch.empty(a.shape, dtype=torch_dtype(dtype_code(ddt)), device="cuda")
-    clk.separable(kernel, torch.from_numpy(a).cuda(), d, N, s)
+    clk.separable(kernel, torch.from_numpy(a).cuda(), d, N, s, defines=defines)
     torch.cuda.synchronize()
     return d.cpu().numpy()
 
@@ -66,6 +66,30 @@ def test_gaussian_to_float_isotropic(clk, oracle, dt):
                 val, scale = oracle.fp64("gaussian_blur_separable_3d", a, N, s)
                 got = run(clk, "gaussian_blur_separable_3d", a, np.float32, N, s)
                 assert close(got, val, scale), (shp, np.dtype(dt), N, s)
+
+
+@pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.int8])
+def test_gaussian_to_integer_bit_exact(clk, oracle, dt):
+    # integer outputs: the reference's tap order, separately rounded products
+    # and sums, IEEE division and a conversion after every pass, bit for bit
+    rng = np.random.default_rng(35)
+    for shp in ((9, 70, 130), (3, 33, 64), (1, 40, 66), (5, 37, 96), (4, 20, 16)):
+        a = random_image(rng, shp, dt)
+        for R in range(1, 9):
+            for sz, cz in ((0.0, 0), (0.8, 1), (1.5, 3)):
+                sig = R / 3.0 + 0.1
+                N = (2 * R + 1, 2 * R + 1, 2 * cz + 1)
+                s = (sig, sig, sz)
+                want = oracle.separable("gaussian_blur_separable_3d", a, dt, N, s)
+                got = run(clk, "gaussian_blur_separable_3d", a, dt, N, s)
+                assert np.array_equal(got, want), (shp, np.dtype(dt), N, s)
+    # the round-half-even conversion policy, every pass
+    a = random_image(rng, (6, 40, 64), dt)
+    for R in (2, 6):
+        N, s = (2 * R + 1, 2 * R + 1, 5), (R / 2.0, R / 2.0, 1.0)
+        want = oracle.separable("gaussian_blur_separable_3d", a, dt, N, s, flags=oracle.FLAG_RTE)
+        got = run(clk, "gaussian_blur_separable_3d", a, dt, N, s, defines={"CLK_CONVERT_ROUNDING": "rte"})
+        assert np.array_equal(got, want), ("rte", np.dtype(dt), N)
 
 
 def test_2d_and_config_shapes(clk, oracle):
