@@ -211,6 +211,30 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
   typedef typename std::conditional<G::SV == 16, uint4, uint2>::type VT;
   S pre[MODE == STAGE_SCALAR ? G::PER : 1];
   VT prev[MODE == STAGE_VEC ? G::PERV : 1];
+  // vector staging: the in-plane offset of each of this thread's staged
+  // vectors -- or, for a vector wholly outside the row, of the row's edge
+  // pixel (bit k of vsplat) -- is the same for every plane: computed once
+  // (the host keeps W * H below 2^32 for this path)
+  uint32_t voff[MODE == STAGE_VEC ? G::PERV : 1];
+  uint32_t vsplat = 0;
+  if constexpr (MODE == STAGE_VEC) {
+#pragma unroll
+    for (int k = 0; k < G::PERV; ++k) {
+      const int sl = tid + k * NT;
+      voff[k] = 0;
+      if (k < G::PERV - 1 || sl < G::NSLOT) {
+        const int r = sl / G::SR, v = sl - r * G::SR;
+        const uint32_t row = (uint32_t)clampi(y0 - R + r, H - 1) * (uint32_t)W;
+        const int gx = x0 - G::RA + v * G::VE;
+        if (gx >= 0 && gx < W) {
+          voff[k] = row + (uint32_t)gx;
+        } else {
+          voff[k] = row + (uint32_t)(gx < 0 ? 0 : W - 1);
+          vsplat |= 1u << k;
+        }
+      }
+    }
+  }
   auto fetch = [&](int zv) {
     const S* sp = src + (int64_t)clampi(zv, Dz - 1) * plane;
     if constexpr (MODE == STAGE_SCALAR) {
@@ -230,13 +254,10 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
       for (int k = 0; k < G::PERV; ++k) {
         const int sl = tid + k * NT;
         if (k < G::PERV - 1 || sl < G::NSLOT) {
-          const int r = sl / G::SR, v = sl - r * G::SR;
-          const S* rowp = sp + (int64_t)clampi(y0 - R + r, H - 1) * W;
-          const int gx = x0 - G::RA + v * G::VE;
-          if (gx >= 0 && gx < W) {
-            prev[k] = __ldg(reinterpret_cast<const VT*>(rowp + gx));
+          if (!(vsplat & (1u << k))) {
+            prev[k] = __ldg(reinterpret_cast<const VT*>(sp + voff[k]));
           } else {
-            const uint32_t w = splat_word<S>(__ldg(rowp + (gx < 0 ? 0 : W - 1)));
+            const uint32_t w = splat_word<S>(__ldg(sp + voff[k]));
             if constexpr (G::SV == 16) prev[k] = make_uint4(w, w, w, w);
             else prev[k] = make_uint2(w, w);
           }
@@ -728,7 +749,7 @@ clk_status launch(const Image& dst, const Image& src, const Params& p, cudaStrea
   constexpr bool PIPE = OP != GAUSS;
   using GV = Geo<S, OP, R, STAGE_VEC, PIPE>;
   if ((uintptr_t)src.ptr % GV::SV == 0 && ((int64_t)src.w * (int64_t)sizeof(S)) % GV::SV == 0 &&
-      smem_ok(k_sep2<S, D, OP, R, STAGE_VEC, PIPE>, GV::smem(p.cz))) {
+      (int64_t)src.w * src.h < (1LL << 32) && smem_ok(k_sep2<S, D, OP, R, STAGE_VEC, PIPE>, GV::smem(p.cz))) {
     k_sep2<S, D, OP, R, STAGE_VEC, PIPE><<<grid, NT, GV::smem(p.cz), st>>>((const S*)src.ptr, (D*)dst.ptr, dst.w,
                                                                            dst.h, dst.d, zchunk, p);
     count_launch();
