@@ -81,7 +81,11 @@ template <int OP, int R> size_t sep2_smem_r(int dt, int cz) {
       case CLK_I16: return sep2_smem_t<int16_t, OP, R>(cz);
     }
     return 0;
-  } else {  // min/max/mean: 8/16-bit pixels
+  } else {  // min/max/mean: 8/16-bit pixels; min/max: float too
+    if (dt == CLK_F32) {
+      if constexpr (OP == SEP_MIN || OP == SEP_MAX) return sep2_smem_t<float, OP, R>(cz);
+      return 0;
+    }
     switch (dt) {
       case CLK_U8: return sep2_smem_t<uint8_t, OP, R>(cz);
       case CLK_U16: return sep2_smem_t<uint16_t, OP, R>(cz);
@@ -323,7 +327,8 @@ ImgStep plan_sep(clk_batch* b, int s, int i, SepDesc* d) {
     const bool s2_int = ints && opn != SEP_GAUSS && R <= 8;
     const bool s2_gauss = fast && R <= 12;
     const bool s2_gx = ints && opn == SEP_GAUSS && R <= 8 && in.dt == out.dt;  // exact order, as the plain path
-    if (s2_int || s2_gauss || s2_gx) {
+    const bool s2_mmf = !ints && out.dt == CLK_F32 && (opn == SEP_MIN || opn == SEP_MAX) && R <= 8;
+    if (s2_int || s2_gauss || s2_gx || s2_mmf) {
       if (!batch_radius(R) || sep2_smem(opn, R, in.dt, cz) > 220 * 1024) return h;  // plain call keeps parity
       d->algo = A_SEP2;
       d->p2.cz = cz;

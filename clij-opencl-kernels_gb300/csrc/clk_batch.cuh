@@ -46,9 +46,13 @@ template <> struct S2Op<SEP_MIN> { static constexpr int v = sep2::MIN; };
 template <> struct S2Op<SEP_MAX> { static constexpr int v = sep2::MAX; };
 template <> struct S2Op<SEP_MEAN> { static constexpr int v = sep2::MEAN; };
 template <> struct S2Op<SEP_GAUSS> { static constexpr int v = sep2::GAUSS; };
-// ... for pixel type T: the Gaussian to 8/16-bit pixels is the exact-order one
+// ... for pixel type T: the Gaussian to 8/16-bit pixels is the exact-order
+// one, float min / max the reference-order ones
 template <int OP, class T> struct S2OpT {
-  static constexpr int v = (OP == SEP_GAUSS && sizeof(T) < 4) ? (int)sep2::GAUSSX : S2Op<OP>::v;
+  static constexpr int v = (OP == SEP_GAUSS && sizeof(T) < 4)  ? (int)sep2::GAUSSX
+                           : (OP == SEP_MIN && sizeof(T) == 4) ? (int)sep2::MINF
+                           : (OP == SEP_MAX && sizeof(T) == 4) ? (int)sep2::MAXF
+                                                               : S2Op<OP>::v;
 };
 
 constexpr int kmax_for(int R) { return R == 0 ? 63 : (2 * R + 1 <= 12 ? 12 : 24); }

@@ -35,6 +35,7 @@ template <> const void* batch_sep2_kernel_op<SEP_MIN>(int R, int dt) {
       case CLK_U8: return (const void*)k_batch_sep2<SEP_MIN, RR, uint8_t>;
       case CLK_U16: return (const void*)k_batch_sep2<SEP_MIN, RR, uint16_t>;
       case CLK_I16: return (const void*)k_batch_sep2<SEP_MIN, RR, int16_t>;
+      case CLK_F32: return (const void*)k_batch_sep2<SEP_MIN, RR, float>;
     }
     return nullptr;
   };

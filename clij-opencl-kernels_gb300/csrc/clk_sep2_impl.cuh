@@ -15,7 +15,10 @@ namespace {
 
 // GAUSSX: the Gaussian to 8/16-bit pixels in the reference's arithmetic
 // (taps in order, separately rounded, IEEE division, dst-typed temporaries)
-enum Op { MIN = 0, MAX = 1, MEAN = 2, GAUSS = 3, GAUSSX = 4 };
+// MINF / MAXF: minimum / maximum of float pixels in the reference's order
+// (start at the centre, then res = min(res, x) for v = -c..c with OpenCL's
+// min: x < res ? x : res), so NaNs and signed zeros come out as they do there
+enum Op { MIN = 0, MAX = 1, MEAN = 2, GAUSS = 3, GAUSSX = 4, MINF = 5, MAXF = 6 };
 
 // temporaries: 16-bit lanes for integer pixels, float for the Gaussian
 template <class S, int OP> struct Temp;
@@ -24,6 +27,21 @@ template <class S> struct Temp<S, MAX> { typedef typename std::conditional<Is16<
 template <class S> struct Temp<S, MEAN> { typedef typename std::conditional<Is16<S>::sgn, int16_t, uint16_t>::type T; };
 template <class S> struct Temp<S, GAUSS> { typedef float T; };
 template <class S> struct Temp<S, GAUSSX> { typedef typename std::conditional<Is16<S>::sgn, int16_t, uint16_t>::type T; };
+template <class S> struct Temp<S, MINF> { typedef float T; };
+template <class S> struct Temp<S, MAXF> { typedef float T; };
+
+// one step of the reference's float min / max loop
+template <int OP> __device__ __forceinline__ float seq_step(float res, float x) {
+  if constexpr (OP == MINF) return x < res ? x : res;
+  else return res < x ? x : res;
+}
+// the reference's loop over a window w[0..2R] (centre w[R]) for one output
+template <int OP, int R> __device__ __forceinline__ float seq_window(const float* w) {
+  float res = w[R];
+#pragma unroll
+  for (int v = 0; v <= 2 * R; ++v) res = seq_step<OP>(res, w[v]);
+  return res;
+}
 
 template <class S, int OP> __device__ __forceinline__ uint32_t mm(uint32_t a, uint32_t b) {
   if constexpr (Is16<S>::sgn) return OP == MIN ? s16x2_min(a, b) : s16x2_max(a, b);
@@ -396,6 +414,18 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
             *reinterpret_cast<uint32_t*>(o0 + j) = __byte_perm(out[j], out[j + 1], 0x5410);
             *reinterpret_cast<uint32_t*>(o1 + j) = __byte_perm(out[j], out[j + 1], 0x7632);
           }
+        } else if constexpr (OP == MINF || OP == MAXF) {
+          float v0[G::WIN_X], v1[G::WIN_X];
+#pragma unroll
+          for (int k = 0; k < G::WIN_X; ++k) {
+            if constexpr (MODE == STAGE_SCALAR) v0[k] = r0[k], v1[k] = r1[k];
+            else v0[k] = __uint_as_float(w0[XOFF + k]), v1[k] = __uint_as_float(w1[XOFF + k]);
+          }
+#pragma unroll
+          for (int j = 0; j < SEGX; j += 2) {
+            *reinterpret_cast<float2*>(o0 + j) = make_float2(seq_window<OP, R>(v0 + j), seq_window<OP, R>(v0 + j + 1));
+            *reinterpret_cast<float2*>(o1 + j) = make_float2(seq_window<OP, R>(v1 + j), seq_window<OP, R>(v1 + j + 1));
+          }
         } else if constexpr (OP == MEAN) {
           int v0[G::WIN_X], v1[G::WIN_X];
 #pragma unroll
@@ -479,6 +509,17 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
         T* o = rs + (sy * SEGY) * TX + 2 * cp;
 #pragma unroll
         for (int j = 0; j < SEGY; ++j) *reinterpret_cast<uint32_t*>(o + j * TX) = out[j];
+      } else if constexpr (OP == MINF || OP == MAXF) {
+        float a[G::WIN_Y], b[G::WIN_Y];  // columns x, x+1
+#pragma unroll
+        for (int k = 0; k < G::WIN_Y; ++k) {
+          const float2 v = *reinterpret_cast<const float2*>(col + k * G::XP);
+          a[k] = v.x, b[k] = v.y;
+        }
+        uint64_t out[SEGY];
+#pragma unroll
+        for (int j = 0; j < SEGY; ++j) out[j] = f2_pack(seq_window<OP, R>(a + j), seq_window<OP, R>(b + j));
+        ring_put2(rs, tid, out);
       } else if constexpr (OP == MEAN) {
         int w0[G::WIN_Y], w1[G::WIN_Y];
 #pragma unroll
@@ -539,7 +580,42 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
       // even widths keep every row pair-aligned: one store for both lanes;
       // odd widths store the lanes separately (the second may lie past W)
       const bool pair = (W & 1) == 0;
-      if constexpr (OP == GAUSSX) {
+      if constexpr (OP == MINF || OP == MAXF) {
+        // the centre plane first, then planes zo-cz .. zo+cz in order
+        const int centre = oldest + cz >= NZ ? oldest + cz - NZ : oldest + cz;
+        uint64_t c[SEGY];
+        ring_get2(ring + (size_t)centre * PL, tid, c);
+        float ra[SEGY], rb[SEGY];
+#pragma unroll
+        for (int j = 0; j < SEGY; ++j) {
+          const float2 f = f2_unpack(c[j]);
+          ra[j] = f.x, rb[j] = f.y;
+        }
+        int idx = oldest;
+        for (int v = 0; v < NZ; ++v) {
+          uint64_t w[SEGY];
+          ring_get2(ring + (size_t)idx * PL, tid, w);
+#pragma unroll
+          for (int j = 0; j < SEGY; ++j) {
+            const float2 f = f2_unpack(w[j]);
+            ra[j] = seq_step<OP>(ra[j], f.x), rb[j] = seq_step<OP>(rb[j], f.y);
+          }
+          idx = idx + 1 == NZ ? 0 : idx + 1;
+        }
+#pragma unroll
+        for (int j = 0; j < SEGY; ++j) {
+          const int gy = y0 + sy * SEGY + j;
+          D* out = dst + (int64_t)zo * plane + (int64_t)gy * W + gx;
+          if (gy < H && gx < W) {
+            if (pair) {
+              *reinterpret_cast<float2*>(out) = make_float2(ra[j], rb[j]);
+            } else {
+              out[0] = ra[j];
+              if (gx + 1 < W) out[1] = rb[j];
+            }
+          }
+        }
+      } else if constexpr (OP == GAUSSX) {
         // planes zo-cz .. zo+cz in order, from the oldest ring slot on
         float2 acc[SEGY];
         int idx = oldest;
@@ -718,7 +794,8 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
 // CTAs per SM the register budget is sized for (64 / 80 / 128 registers;
 // the vector staging holds fewer prefetch registers than the scalar one)
 template <int OP, int MODE> constexpr int min_ctas() {
-  return OP == GAUSS ? 2 : OP == GAUSSX ? (MODE == STAGE_VEC ? 3 : 2) : MODE == STAGE_VEC ? 4 : 3;
+  return (OP == GAUSS || OP == MINF || OP == MAXF) ? 2 : OP == GAUSSX ? (MODE == STAGE_VEC ? 3 : 2)
+                                                     : MODE == STAGE_VEC ? 4 : 3;
 }
 
 template <class S, class D, int OP, int R, int MODE, bool PIPE = false>
@@ -784,7 +861,7 @@ clk_status launch(const Image& dst, const Image& src, const Params& p, cudaStrea
   // vector staging when the image base and rows are aligned to its vectors;
   // the pipelined loop (double-buffered tiles, one barrier per plane) where
   // its shared memory leaves several CTAs per SM: min / max / mean
-  constexpr bool PIPE = OP != GAUSS;
+  constexpr bool PIPE = OP != GAUSS && OP != MINF && OP != MAXF;  // float tiles: one buffer each
   using GV = Geo<S, OP, R, STAGE_VEC, PIPE>;
   if ((uintptr_t)src.ptr % GV::SV == 0 && ((int64_t)src.w * (int64_t)sizeof(S)) % GV::SV == 0 &&
       (int64_t)src.w * src.h < (1LL << 32) && smem_ok(k_sep2<S, D, OP, R, STAGE_VEC, PIPE>, GV::smem(p.cz))) {

@@ -1,5 +1,6 @@
 // clk_sep2_minmax.cu - instantiations of the fused separable kernel (clk_sep2_impl.cuh)
-// for minimum/maximum_separable on 8/16-bit pixels.
+// for minimum/maximum_separable on 8/16-bit pixels (16-bit SIMD lanes) and
+// float pixels (the reference's comparison order).
 #include "clk_sep2_impl.cuh"
 
 namespace clk {
@@ -23,6 +24,9 @@ clk_status sep2_minmax(bool is_max, int R, const Image& dst, const Image& src, i
     case CLK_I8:
       return is_max ? by_radius<int8_t, int8_t, MAX, kMaxRIntegers>(R, dst, src, p, st)
                     : by_radius<int8_t, int8_t, MIN, kMaxRIntegers>(R, dst, src, p, st);
+    case CLK_F32:  // the reference's comparison order
+      return is_max ? by_radius<float, float, MAXF, kMaxRIntegers>(R, dst, src, p, st)
+                    : by_radius<float, float, MINF, kMaxRIntegers>(R, dst, src, p, st);
   }
   return CLK_UNSUPPORTED_DTYPE;
 }

@@ -112,7 +112,7 @@ clk_status fused_separable(SepOp op, const Image& dst, const Image& src, const S
     const int R = ft.c[0], cz = ft.c[2];
     const bool ints = src.dt == dst.dt && src.dt != CLK_F32;
     clk_status s2 = CLK_UNSUPPORTED_DTYPE;
-    if ((op == SEP_MIN || op == SEP_MAX) && ints) {
+    if ((op == SEP_MIN || op == SEP_MAX) && (ints || (src.dt == CLK_F32 && dst.dt == CLK_F32))) {
       s2 = sep2_minmax(op == SEP_MAX, R, dst, src, cz, st);
     } else if (op == SEP_MEAN && ints) {
       s2 = sep2_mean(R, dst, src, cz, st);

@@ -68,6 +68,27 @@ def test_gaussian_to_float_isotropic(clk, oracle, dt):
                 assert close(got, val, scale), (shp, np.dtype(dt), N, s)
 
 
+@pytest.mark.parametrize("kernel", ["minimum_separable_3d", "maximum_separable_3d"])
+def test_float_min_max_reference_order(clk, oracle, kernel):
+    # float pixels with NaNs and signed zeros: the reference's loop (start at
+    # the centre, res = min(res, x) in tap order) decides which NaN / zero
+    # survives; compared bit for bit
+    rng = np.random.default_rng(36)
+    for shp in ((9, 70, 130), (3, 33, 64), (5, 37, 96), (1, 40, 66)):
+        a = (rng.standard_normal(shp) * 100).astype(np.float32)
+        a[rng.random(shp) < 0.02] = np.nan
+        a[rng.random(shp) < 0.05] = 0.0
+        a[rng.random(shp) < 0.05] = -0.0
+        a[rng.random(shp) < 0.01] = np.inf
+        a[rng.random(shp) < 0.01] = -np.inf
+        for R in (1, 2, 4, 5, 8):
+            for rz in (0, 1, 3):
+                N = (2 * R + 1, 2 * R + 1, 2 * rz + 1)
+                want = oracle.separable(kernel, a, np.float32, N, (R, R, rz))
+                got = run(clk, kernel, a, np.float32, N, (R, R, rz))
+                assert got.tobytes() == want.tobytes(), (kernel, shp, N)
+
+
 @pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.int8])
 def test_gaussian_to_integer_bit_exact(clk, oracle, dt):
     # integer outputs: the reference's tap order, separately rounded products
