@@ -477,6 +477,10 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
         st = fast_gradient(k->sub - ST_GRADIENT_X, dst, src, pol, s);
         if (st != CLK_UNSUPPORTED_DTYPE) return st;
       }
+      if (full && k->sub >= ST_LAPLACE_DIAMOND_2D) {
+        st = fast_laplace(k->sub, dst, src, pol, s);
+        if (st != CLK_UNSUPPORTED_DTYPE) return st;
+      }
       return direct_stencil((StencilKind)k->sub, dst, src, r, pol, s);
     }
     case F_THRESH:

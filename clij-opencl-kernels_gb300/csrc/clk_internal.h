@@ -120,6 +120,9 @@ clk_status fast_pointwise(bool greater, const Image& dst, const Image& src, floa
                           cudaStream_t st);
 // gradient along axis 0/1/2 over whole rows (width a multiple of 8, aligned)
 clk_status fast_gradient(int axis, const Image& dst, const Image& src, const Policy& p, cudaStream_t st);
+// laplace_diamond_{2d,3d} / laplace_box_2d (integer pixels) and laplace_box_3d
+// (signed integer pixels) over whole images, row-vectorised
+clk_status fast_laplace(int kind, const Image& dst, const Image& src, const Policy& p, cudaStream_t st);
 clk_status direct_morph(bool erode, bool sphere, const Image& dst, const Image& src, Range r, const Policy& p,
                         cudaStream_t st, bool planar = false);
 clk_status direct_sobel(const Image& dst, const Image& src, Range r, const Policy& p, cudaStream_t st);

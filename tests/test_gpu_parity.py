@@ -160,6 +160,22 @@ def test_sobel3d_unsigned_wrap_counts_with_zero_pixels(clk, oracle):
             assert_fp64_close(got, val, scale, f"sobel_3d {shp} {np.dtype(sdt)} zero border")
 
 
+@pytest.mark.parametrize("kernel", ["laplace_diamond_2d", "laplace_box_2d", "laplace_diamond_3d", "laplace_box_3d"])
+def test_laplace_row_path(clk, oracle, kernel):
+    # widths that are whole 8-pixel vectors take the row kernels (integer
+    # pixels; laplace_box_3d for signed ones), bit-exact; thin stacks, one
+    # row, one plane, every pixel-type pair into float and into the source type
+    rng = np.random.default_rng(7)
+    shapes = [(33, 64), (1, 8), (7, 40)] if kernel.endswith("2d") else [(5, 33, 64), (1, 9, 16), (4, 1, 8), (6, 20, 96)]
+    for shp in shapes:
+        for sdt in DTYPES:
+            a = random_image(rng, shp, sdt)
+            for ddt in (np.float32, sdt):
+                got = run_execute(clk, kernel, a, ddt, {})
+                want = oracle.execute(kernel, a, ddt)
+                assert got.tobytes() == want.tobytes(), (kernel, shp, np.dtype(sdt), np.dtype(ddt))
+
+
 def test_partial_global_range_writes_only_that_box(clk, oracle):
     rng = np.random.default_rng(5)
     a = random_image(rng, (6, 10, 12), np.uint16)
