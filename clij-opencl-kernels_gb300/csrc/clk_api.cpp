@@ -481,6 +481,10 @@ clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t narg
         st = fast_laplace(k->sub, dst, src, pol, s);
         if (st != CLK_UNSUPPORTED_DTYPE) return st;
       }
+      if (full && k->sub == ST_LAPLACE_BOX_3D) {
+        st = fast_laplace_box3d(dst, src, pol, s);
+        if (st != CLK_UNSUPPORTED_DTYPE) return st;
+      }
       return direct_stencil((StencilKind)k->sub, dst, src, r, pol, s);
     }
     case F_THRESH:

@@ -222,6 +222,101 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// The same sum over whole images, tiled: a CTA owns 128 x 8 outputs of a
+// z-chunk; each staged input plane holds t(v) = (float)(v * -1) of every
+// pixel of the (8+2) x (128+2) halo region once (the conversion that the
+// per-voxel kernel repeats for 26 taps); a thread takes four consecutive
+// outputs of a row, keeps the 9 (y, z) rows of its 6 columns in registers
+// and adds the 27 taps in the reference's order (ax, ay, az, az fastest),
+// the centre as (float)v.  Planes sit in a ring of four slots (plane p in
+// slot p & 3) so each plane costs one barrier; the next plane's pixels are
+// loaded before the current plane's sums.
+constexpr int LBX = 128, LBY = 8, LBP = LBX + 4;  // tile, staged row pitch (floats; 130 used)
+template <class S, class D>
+__global__ void __launch_bounds__(256)
+    k_laplace_box3d_tile(D* __restrict__ dst, const S* __restrict__ src, int W, int H, int Dz, int zchunk, bool rte) {
+  __shared__ __align__(16) float ring[4][(LBY + 2) * LBP];
+  constexpr int NS = (LBY + 2) * (LBX + 2), PER = (NS + 255) / 256;
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  const int x0 = blockIdx.x * LBX, y0 = blockIdx.y * LBY;
+  const int z0 = blockIdx.z * zchunk, z1 = min(Dz, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+  const int xo = x0 + 4 * tx, yo = y0 + ty;  // this thread's first output
+  // staged cell i <-> region row i / (LBX + 2), column i % (LBX + 2); the
+  // in-plane offset of its clamped pixel is the same for every plane
+  int soff[PER];
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int i = tid + k * 256;
+    const int r = i / (LBX + 2), c = i - r * (LBX + 2);
+    soff[k] = i < NS ? clampi(y0 - 1 + r, H - 1) * W + clampi(x0 - 1 + c, W - 1) : 0;
+  }
+  decltype(readx(src, 0)) pre[PER];
+  auto fetch = [&](int p) {
+    const S* sp = src + (int64_t)clampi(p, Dz - 1) * plane;
+#pragma unroll
+    for (int k = 0; k < PER; ++k)
+      if (tid + k * 256 < NS) pre[k] = readx(sp, soff[k]);
+  };
+  auto commit = [&](int p) {
+    float* t = ring[p & 3];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int i = tid + k * 256;
+      if (i < NS) {
+        const int r = i / (LBX + 2), c = i - r * (LBX + 2);
+        t[r * LBP + c] = (float)(pre[k] * -1);
+      }
+    }
+  };
+  // planes z0-1 .. z0+1 staged before the first output plane
+  for (int p = z0 - 1; p <= z0 + 1; ++p) {
+    fetch(p);
+    commit(p);
+  }
+  __syncthreads();
+  for (int z = z0; z < z1; ++z) {
+    const bool more = z + 1 < z1;
+    if (more) fetch(z + 2);
+    // centres, as (float)v
+    float cen[4];
+    const S* cp = src + (int64_t)z * plane + (int64_t)min(yo, H - 1) * W;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) cen[k] = (float)readx(cp, min(xo + k, W - 1));
+    // the 9 (y, z) rows of columns xo-1 .. xo+4 (region columns 4tx .. 4tx+5)
+    float v[3][3][6];  // [ay][az][column]
+#pragma unroll
+    for (int az = 0; az < 3; ++az) {
+      const float* t = ring[(z - 1 + az) & 3];
+#pragma unroll
+      for (int ay = 0; ay < 3; ++ay) {
+        const float* row = t + (ty + ay) * LBP + 4 * tx;
+        const float4 a = *reinterpret_cast<const float4*>(row);
+        const float2 b = *reinterpret_cast<const float2*>(row + 4);
+        v[ay][az][0] = a.x, v[ay][az][1] = a.y, v[ay][az][2] = a.z, v[ay][az][3] = a.w;
+        v[ay][az][4] = b.x, v[ay][az][5] = b.y;
+      }
+    }
+    if (yo < H) {
+      D* o = dst + (int64_t)z * plane + (int64_t)yo * W;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        float result = 0.f;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+          for (int ay = 0; ay < 3; ++ay)
+#pragma unroll
+            for (int az = 0; az < 3; ++az)
+              result = __fadd_rn(result, (ax == 1 && ay == 1 && az == 1) ? cen[k] : v[ay][az][k + ax]);
+        if (xo + k < W) o[xo + k] = convert_sat<D>(result, rte);
+      }
+    }
+    if (more) commit(z + 2);
+    __syncthreads();
+  }
+}
+
 // convolve_{2d,3d}_x.cl:17-31: c = kernel extent / 2; x, y, z over -c..c:
 // sum = sum + kernel(c + offset) * src(coord + offset), float multiply then
 // float add (no contraction), both reads clamped; CONVERT(sum).
@@ -447,6 +542,28 @@ clk_status direct_stencil(StencilKind kind, const Image& dst, const Image& src, 
   if (!ok) return fail(CLK_UNSUPPORTED_DTYPE, "stencil: pixel types %d -> %d", src.dt, dst.dt);
   count_launch();
   return check_launch("stencil");
+}
+
+clk_status fast_laplace_box3d(const Image& dst, const Image& src, const Policy& p, cudaStream_t st) {
+  if (src.w != dst.w || src.h != dst.h || src.d != dst.d || (int64_t)src.w * src.h >= (1LL << 31))
+    return CLK_UNSUPPORTED_DTYPE;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int tx = (src.w + LBX - 1) / LBX, ty = (src.h + LBY - 1) / LBY;
+  int chunks = 1;
+  while ((int64_t)tx * ty * chunks < 4LL * sms && src.d / (chunks * 2) >= 8) chunks *= 2;
+  const int zchunk = (src.d + chunks - 1) / chunks;
+  const dim3 grid(tx, ty, (src.d + zchunk - 1) / zchunk);
+  const bool ok = dispatch_types(src.dt, dst.dt, [&](auto s, auto d) {
+    using S = decltype(s);
+    using D = decltype(d);
+    k_laplace_box3d_tile<S, D><<<grid, 256, 0, st>>>((D*)dst.ptr, (const S*)src.ptr, src.w, src.h, src.d, zchunk,
+                                                     p.rte);
+  });
+  if (!ok) return CLK_UNSUPPORTED_DTYPE;
+  count_launch();
+  return check_launch("laplace_box_3d (tiles)");
 }
 
 clk_status direct_convolve(const Image& dst, const Image& src, const Image& kern, Range r, const Policy& p,

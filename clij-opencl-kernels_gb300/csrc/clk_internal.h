@@ -123,6 +123,8 @@ clk_status fast_gradient(int axis, const Image& dst, const Image& src, const Pol
 // laplace_diamond_{2d,3d} / laplace_box_2d (integer pixels) and laplace_box_3d
 // (signed integer pixels) over whole images, row-vectorised
 clk_status fast_laplace(int kind, const Image& dst, const Image& src, const Policy& p, cudaStream_t st);
+// laplace_box_3d over whole images, every pixel type, in the reference's order
+clk_status fast_laplace_box3d(const Image& dst, const Image& src, const Policy& p, cudaStream_t st);
 clk_status direct_morph(bool erode, bool sphere, const Image& dst, const Image& src, Range r, const Policy& p,
                         cudaStream_t st, bool planar = false);
 clk_status direct_sobel(const Image& dst, const Image& src, Range r, const Policy& p, cudaStream_t st);
