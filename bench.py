@@ -52,6 +52,9 @@ NCU_DRAM_BYTES_PER_VOXEL = {
 NCU_ALU_PIPE_BUSY = {"median_box r1": 0.80, "median_sphere r2": 0.78}
 
 
+NOMINAL_HBM_GBS = 7900.0  # GB300 HBM3e, nominal (the measured copy peak is the roofline)
+
+
 def suite_spec():
     """(name, kind, kernel, params, src, dst dtype code, bytes/voxel)."""
     return [
@@ -829,6 +832,7 @@ def main():
             "per_filter": per,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(dom_gbs, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(dom_gbs / peak, 4), "peak_kind": peak_kind,
+                         "frac_of_nominal": round(dom_gbs / NOMINAL_HBM_GBS, 4),
                          "traffic": (round(NCU_DRAM_BYTES_PER_VOXEL[dom] * V) if dom in NCU_DRAM_BYTES_PER_VOXEL
                                      else None),
                          "algorithmic_bytes": int(V * per[dom]["bytes_per_voxel"]),
