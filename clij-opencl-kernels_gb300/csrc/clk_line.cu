@@ -169,8 +169,91 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
     return r;
   };
 
-  Lane<OP, T> acc[M], win[M];
   const int base = g * M;  // staged line of tap k = 0 for output j = 0 is base + j
+  // outputs: lines l0 + base + j, columns c0 + ca / c0 + cb
+  auto store_out = [&](const D (&ra)[M], const D (&rb)[M]) {
+    if constexpr (AXIS == 0) {
+      // the lanes are rows: transpose through shared memory so that the
+      // stores run along x
+      D* so = reinterpret_cast<D*>(smem_raw);
+      constexpr int OP_ = TL + 1;  // odd pitch
+      __syncthreads();             // everyone is done with the staged tile
+#pragma unroll
+      for (int j = 0; j < M; ++j) so[ca * OP_ + base + j] = ra[j], so[cb * OP_ + base + j] = rb[j];
+      __syncthreads();
+      for (int c = warp; c < TC; c += NT / 32) {
+        if (c0 + c >= C) break;
+#pragma unroll
+        for (int h = 0; h < TL / 32; ++h) {
+          const int l = lane + 32 * h;
+          if (l0 + l < L) dst[at(l0 + l, c0 + c)] = so[c * OP_ + l];
+        }
+      }
+    } else {
+      // adjacent pair as one store where the rows keep pairs aligned
+      const bool pair = (W & 1) == 0 && c0 + cb < C && ((uintptr_t)dst & (2 * sizeof(D) - 1)) == 0;
+#pragma unroll
+      for (int j = 0; j < M; ++j) {
+        const int l = l0 + base + j;
+        if (l >= L) break;
+        D* o = dst + at(l, c0 + ca);
+        if (pair) {
+          store_pair(o, ra[j], rb[j]);
+        } else {
+          if (c0 + ca < C) o[0] = ra[j];
+          if (c0 + cb < C) o[1] = rb[j];
+        }
+      }
+    }
+  };
+  if constexpr (OP == MIN || OP == MAX) {
+    if (2 * R >= M) {
+      // van Herk / Gil-Werman over the window lines base .. base+2R+M-1:
+      // out[j] = first(suffix of lines j..M-1, prefix of lines M..j+2R),
+      // with first(a, b) = the earlier operand unless the later one is
+      // strictly smaller (MIN) / larger (MAX) or the earlier one is NaN --
+      // an associative "leftmost extreme, NaN never chosen".  The
+      // reference's loop (res = centre, then res = x < res ? x : res over
+      // the taps) returns the leftmost extreme of (centre, taps), or NaN
+      // when the centre is NaN: first(centre, out[j]) unless the centre is
+      // NaN.  2R + 2M - 2 operations for M outputs instead of (2R+1) M.
+      auto first = [](T a, T b) -> T {
+        if constexpr (std::is_same<T, float>::value) {
+          const bool take = (OP == MIN ? b < a : a < b) || a != a;
+          return take ? b : a;
+        } else {
+          return OP == MIN ? (b < a ? b : a) : (a < b ? b : a);
+        }
+      };
+      auto firstl = [&](const Lane<OP, T>& a, const Lane<OP, T>& b) {
+        Lane<OP, T> r;
+        r.a = first(a.a, b.a), r.b = first(a.b, b.b);
+        return r;
+      };
+      Lane<OP, T> suf[M];
+      suf[M - 1] = get(base + M - 1);
+#pragma unroll
+      for (int j = M - 2; j >= 0; --j) suf[j] = firstl(get(base + j), suf[j + 1]);
+      Lane<OP, T> pre = get(base + M);
+      for (int k = M + 1; k < 2 * R; ++k) pre = firstl(pre, get(base + k));
+      D ra[M], rb[M];
+#pragma unroll
+      for (int t = 0; t < M; ++t) {
+        const int k = 2 * R + t;
+        if (k > M) pre = firstl(pre, get(base + k));
+        Lane<OP, T> o = firstl(suf[t], pre);
+        if constexpr (std::is_same<T, float>::value) {  // the centre first, unless it is NaN
+          const Lane<OP, T> c = get(base + t + R);
+          o.a = c.a != c.a ? c.a : first(c.a, o.a);
+          o.b = c.b != c.b ? c.b : first(c.b, o.b);
+        }
+        ra[t] = (D)o.a, rb[t] = (D)o.b;
+      }
+      store_out(ra, rb);
+      return;
+    }
+  }
+  Lane<OP, T> acc[M], win[M];
 #pragma unroll
   for (int j = 0; j < M; ++j) {
     if constexpr (OP == MIN || OP == MAX) acc[j] = get(base + j + R);  // the centre
@@ -227,39 +310,7 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
       ra[j] = (D)acc[j].a, rb[j] = (D)acc[j].b;
     }
   }
-  if constexpr (AXIS == 0) {
-    // the lanes are rows: transpose through shared memory so that the
-    // stores run along x
-    D* so = reinterpret_cast<D*>(smem_raw);
-    constexpr int OP_ = TL + 1;  // odd pitch
-    __syncthreads();             // everyone is done with the staged tile
-#pragma unroll
-    for (int j = 0; j < M; ++j) so[ca * OP_ + base + j] = ra[j], so[cb * OP_ + base + j] = rb[j];
-    __syncthreads();
-    for (int c = warp; c < TC; c += NT / 32) {
-      if (c0 + c >= C) break;
-#pragma unroll
-      for (int h = 0; h < TL / 32; ++h) {
-        const int l = lane + 32 * h;
-        if (l0 + l < L) dst[at(l0 + l, c0 + c)] = so[c * OP_ + l];
-      }
-    }
-  } else {
-    // adjacent pair as one store where the rows keep pairs aligned
-    const bool pair = (W & 1) == 0 && c0 + cb < C && ((uintptr_t)dst & (2 * sizeof(D) - 1)) == 0;
-#pragma unroll
-    for (int j = 0; j < M; ++j) {
-      const int l = l0 + base + j;
-      if (l >= L) break;
-      D* o = dst + at(l, c0 + ca);
-      if (pair) {
-        store_pair(o, ra[j], rb[j]);
-      } else {
-        if (c0 + ca < C) o[0] = ra[j];
-        if (c0 + cb < C) o[1] = rb[j];
-      }
-    }
-  }
+  store_out(ra, rb);
 }
 
 template <class S, class D, int OP>

@@ -55,11 +55,18 @@ def test_float_minmax_large_radii_with_nan(clk, oracle, kernel):
     for shp in SHAPES:
         a = random_image(rng, shp, np.float32)
         a.flat[rng.integers(0, a.size, 5)] = np.nan
-        for r in RADII:
-            N = tuple(2 * v + 1 for v in r)
-            want = oracle.separable(kernel, a, np.float32, N, tuple(float(v) for v in r))
-            got = run(clk, kernel, a, np.float32, N, tuple(float(v) for v in r))
-            assert np.array_equal(got, want, equal_nan=True), (kernel, shp, N)
+        b = a.copy()  # dense NaNs, signed zeros and infinities: which one survives is the loop order's
+        b[rng.random(shp) < 0.05] = np.nan
+        b[rng.random(shp) < 0.1] = 0.0
+        b[rng.random(shp) < 0.1] = -0.0
+        b[rng.random(shp) < 0.02] = np.inf
+        b[rng.random(shp) < 0.02] = -np.inf
+        for img in (a, b):
+            for r in RADII:
+                N = tuple(2 * v + 1 for v in r)
+                want = oracle.separable(kernel, img, np.float32, N, tuple(float(v) for v in r))
+                got = run(clk, kernel, img, np.float32, N, tuple(float(v) for v in r))
+                assert got.tobytes() == want.tobytes(), (kernel, shp, N)
 
 
 @pytest.mark.parametrize("dt", [np.uint16, np.int8, np.float32])
