@@ -42,6 +42,41 @@ template <int OP, int R> __device__ __forceinline__ float seq_window(const float
   for (int v = 0; v <= 2 * R; ++v) res = seq_step<OP>(res, w[v]);
   return res;
 }
+// "the earlier operand unless the later one is strictly more extreme or the
+// earlier one is NaN": associative (the leftmost extreme, NaN never chosen)
+template <int OP> __device__ __forceinline__ float first_op(float a, float b) {
+  const bool take = (OP == MINF ? b < a : a < b) || a != a;
+  return take ? b : a;
+}
+// The reference's loop for M consecutive outputs over w[0 .. M+2R-1]: the
+// leftmost extreme of each window by the van Herk / Gil-Werman split
+// (2R + 2M - 2 operations), then the centre first unless it is NaN -- equal
+// to seq_window bit for bit (NaNs and signed zeros included).
+template <int OP, int M, int R> __device__ __forceinline__ void window_first(const float* w, float (&out)[M]) {
+  if constexpr (2 * R >= M && M > 1) {
+    float suf[M];
+    suf[M - 1] = w[M - 1];
+#pragma unroll
+    for (int j = M - 2; j >= 0; --j) suf[j] = first_op<OP>(w[j], suf[j + 1]);
+    float pre = w[M];
+#pragma unroll
+    for (int k = M + 1; k <= 2 * R; ++k) pre = first_op<OP>(pre, w[k]);
+    out[0] = first_op<OP>(suf[0], pre);
+#pragma unroll
+    for (int j = 1; j < M; ++j) {
+      pre = first_op<OP>(pre, w[j + 2 * R]);
+      out[j] = first_op<OP>(suf[j], pre);
+    }
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+      const float c = w[j + R];
+      out[j] = c != c ? c : first_op<OP>(c, out[j]);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < M; ++j) out[j] = seq_window<OP, R>(w + j);
+  }
+}
 
 template <class S, int OP> __device__ __forceinline__ uint32_t mm(uint32_t a, uint32_t b) {
   if constexpr (Is16<S>::sgn) return OP == MIN ? s16x2_min(a, b) : s16x2_max(a, b);
@@ -421,10 +456,13 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
             if constexpr (MODE == STAGE_SCALAR) v0[k] = r0[k], v1[k] = r1[k];
             else v0[k] = __uint_as_float(w0[XOFF + k]), v1[k] = __uint_as_float(w1[XOFF + k]);
           }
+          float q0[SEGX], q1[SEGX];
+          window_first<OP, SEGX, R>(v0, q0);
+          window_first<OP, SEGX, R>(v1, q1);
 #pragma unroll
           for (int j = 0; j < SEGX; j += 2) {
-            *reinterpret_cast<float2*>(o0 + j) = make_float2(seq_window<OP, R>(v0 + j), seq_window<OP, R>(v0 + j + 1));
-            *reinterpret_cast<float2*>(o1 + j) = make_float2(seq_window<OP, R>(v1 + j), seq_window<OP, R>(v1 + j + 1));
+            *reinterpret_cast<float2*>(o0 + j) = make_float2(q0[j], q0[j + 1]);
+            *reinterpret_cast<float2*>(o1 + j) = make_float2(q1[j], q1[j + 1]);
           }
         } else if constexpr (OP == MEAN) {
           int v0[G::WIN_X], v1[G::WIN_X];
@@ -516,9 +554,12 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
           const float2 v = *reinterpret_cast<const float2*>(col + k * G::XP);
           a[k] = v.x, b[k] = v.y;
         }
+        float qa[SEGY], qb[SEGY];
+        window_first<OP, SEGY, R>(a, qa);
+        window_first<OP, SEGY, R>(b, qb);
         uint64_t out[SEGY];
 #pragma unroll
-        for (int j = 0; j < SEGY; ++j) out[j] = f2_pack(seq_window<OP, R>(a + j), seq_window<OP, R>(b + j));
+        for (int j = 0; j < SEGY; ++j) out[j] = f2_pack(qa[j], qb[j]);
         ring_put2(rs, tid, out);
       } else if constexpr (OP == MEAN) {
         int w0[G::WIN_Y], w1[G::WIN_Y];
