@@ -41,7 +41,7 @@ def _rank(rank, ws, port, out):
 
 def test_max_over_ranks_and_aggregate_throughput():
     ws, port = 2, _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of this (multi-threaded) process
         out = m.dict()
         mp.spawn(_rank, args=(ws, port, out), nprocs=ws, join=True)
         res = dict(out)
