@@ -45,14 +45,18 @@ template <bool ERODE> __device__ __forceinline__ uint4 comb(uint4 a, uint4 b) {
 }
 
 // x-neighbour combination of chunk c with the left/right neighbour chunks
-// (their boundary bytes); at the image's first/last chunk the clamped
-// neighbour is the chunk's own boundary byte.
+// (their boundary bytes: the last word of the left chunk, the first of the
+// right one); at the image's first/last chunk the clamped neighbour is the
+// chunk's own boundary byte.
 template <bool ERODE>
-__device__ __forceinline__ uint4 xcomb(uint4 c, uint4 l, uint4 r, bool first, bool last) {
-  const uint32_t lb = first ? (c.x & 0xFFu) : (l.w >> 24);
-  const uint32_t rb = last ? (c.w >> 24) : (r.x & 0xFFu);
+__device__ __forceinline__ uint4 xcomb(uint4 c, uint32_t lw, uint32_t rx, bool first, bool last) {
+  const uint32_t lb = first ? (c.x & 0xFFu) : (lw >> 24);
+  const uint32_t rb = last ? (c.w >> 24) : (rx & 0xFFu);
   return comb<ERODE>(comb<ERODE>(c, shl1(c, lb)), shr1(c, rb));
 }
+// the boundary words of the chunks left / right of chunk i (4-byte reads)
+__device__ __forceinline__ uint32_t lword(const uint4* P, int i) { return reinterpret_cast<const uint32_t*>(P + i - 1)[3]; }
+__device__ __forceinline__ uint32_t rword(const uint4* P, int i) { return reinterpret_cast<const uint32_t*>(P + i + 1)[0]; }
 
 // One r=1 step at tile chunk (r, q) of a region whose planes A (z-1), B (z),
 // C (z+1) are stored with row pitch `pitch` and one halo chunk/row around.
@@ -62,13 +66,13 @@ __device__ __forceinline__ uint4 step(const uint4* A, const uint4* B, const uint
   const int i = (r + 1) * pitch + (q + 1);
   if constexpr (SPHERE) {
     const uint4 c = B[i];
-    uint4 o = xcomb<ERODE>(c, B[i - 1], B[i + 1], first, last);
+    uint4 o = xcomb<ERODE>(c, lword(B, i), rword(B, i), first, last);
     o = comb<ERODE>(o, B[i - pitch]);
     o = comb<ERODE>(o, B[i + pitch]);
     o = comb<ERODE>(o, A[i]);
     return comb<ERODE>(o, C[i]);
   } else {
-    uint4 o = xcomb<ERODE>(B[i], B[i - 1], B[i + 1], first, last);
+    uint4 o = xcomb<ERODE>(B[i], lword(B, i), rword(B, i), first, last);
 #pragma unroll
     for (int dy = -1; dy <= 1; ++dy) {
       const uint4* pl[3] = {A, B, C};
@@ -76,7 +80,7 @@ __device__ __forceinline__ uint4 step(const uint4* A, const uint4* B, const uint
       for (int p = 0; p < 3; ++p) {
         if (p == 1 && dy == 0) continue;
         const int j = i + dy * pitch;
-        o = comb<ERODE>(o, xcomb<ERODE>(pl[p][j], pl[p][j - 1], pl[p][j + 1], first, last));
+        o = comb<ERODE>(o, xcomb<ERODE>(pl[p][j], lword(pl[p], j), rword(pl[p], j), first, last));
       }
     }
     return o;
