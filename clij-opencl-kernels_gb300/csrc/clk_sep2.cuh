@@ -11,14 +11,19 @@
 //           for two outputs and the window slides along x in registers;
 //   Y pass  a thread filters a column pair x 4 outputs, lanes = (x, x+1);
 //   Z pass  the Y results enter a ring of the last 2cz+1 planes (shared
-//           memory); the same thread reduces its cells along z and writes
-//           two outputs with one store.
-// Lane types: min/max on 8/16-bit pixels use min/max.{u,s}16x2, the mean
-// sums int32 lanes and divides exactly (a 64-bit reciprocal multiply that
-// equals truncating fl(S/N) for |S| < 2^24, N < 256), the Gaussian uses
-// fma.rn.f32x2 with weights pre-divided by their sum, folded symmetrically.
-// Integer temporaries keep the dst pixel type between passes, so integer
-// results equal three launches of the reference kernels bit for bit.
+//           memory, private to the thread); the same thread reduces its
+//           cells along z and writes two outputs with one store.
+// Operations: min/max on 8/16-bit pixels use min/max.{u,s}16x2 with the van
+// Herk split; float min/max follow the reference's comparison order (the
+// van Herk split with its leftmost-extreme tie rule, the centre first); the
+// mean sums int32 lanes and divides exactly (a 32-bit reciprocal multiply
+// that equals truncating fl(S/N) for |S| < 2^24, N < 256); the Gaussian to
+// float uses fma.rn.f32x2 with weights pre-divided by their sum, folded
+// symmetrically; the Gaussian to 8/16-bit pixels keeps the reference's
+// arithmetic (taps in order, separately rounded products and sums, IEEE
+// division).  Integer temporaries keep the dst pixel type between passes,
+// so integer results equal three launches of the reference kernels bit for
+// bit.
 #pragma once
 #include "clk_common.cuh"
 
