@@ -1,5 +1,7 @@
 // clk_median.cu - fast median_box_3d 3x3x3, median_sphere_3d radius 2
-// (33 voxels) and median_box_2d 3x3 for 8/16-bit integer images.
+// (33 voxels) and median_box_2d 3x3 (also the 3x3 of every plane of the
+// slice-by-slice box) for 8/16-bit integer images and, on 32-bit
+// order-preserving keys, float images.
 //
 // The reference gathers the neighbourhood into an array and insertion-sorts
 // it per voxel (median_box_3d_x.cl:3-20, median_sphere_3d_x.cl:3-20); the
@@ -14,7 +16,10 @@
 //    outputs once (three sorted columns merged into a sorted 9), which the
 //    outputs of the planes above and below reuse;
 //  * box: the merge of planes z and z+1 (ranks 4..13) serves the outputs at
-//    z and z+1; each then needs one rank-9 selection against the third plane.
+//    z and z+1; each then needs one rank-9 selection against the third plane;
+//  * sphere (8/16-bit): likewise the merge of planes z and z+1 (16 ranks)
+//    serves z and z+1, each adding its other plane's block and six singles;
+//  * the next z-pair's planes are loaded before the current pair's networks.
 // Borders clamp exactly as the reference's reads do.
 #include "clk_median_impl.cuh"
 
