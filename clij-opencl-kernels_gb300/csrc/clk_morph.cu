@@ -233,12 +233,12 @@ clk_status launch_morph(const Image& dst, const Image& src, cudaStream_t st) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int chunks = 1;
-  // z-chunks: enough CTAs for 8 per SM (r=1); the fused radius 2, whose
-  // chunks re-stage two more input planes each, is faster with half as many
-  // (measured: 0.234 against 0.240 ms on 1024x1024x256; r=1 0.135 against
-  // 0.117 ms the other way)
-  const int64_t want = (ITER == 2 ? 4LL : 8LL) * sms;
-  while ((int64_t)tx * ty * chunks < want && src.d / (chunks * 2) >= 16) chunks *= 2;
+  // z-chunks: enough CTAs for 16 per SM (r=1: 0.115 ms on 1024x1024x256
+  // against 0.117 with 8 and 0.135 with 4); the fused radius 2, whose
+  // chunks re-stage two more input planes each, is faster with 4 (0.234
+  // against 0.240 ms with 8)
+  const int64_t want = (ITER == 2 ? 4LL : 16LL) * sms;
+  while ((int64_t)tx * ty * chunks < want && src.d / (chunks * 2) >= 8) chunks *= 2;
   const int zchunk = (src.d + chunks - 1) / chunks;
   dim3 grid(tx, ty, (src.d + zchunk - 1) / zchunk);
   using G = Geo<ITER>;
