@@ -99,6 +99,10 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// READ(..).x * -1 in the read's own type: for the uint reads of unsigned
+// pixels the product wraps to 2^32 - v (0 stays 0), as the reference's does
+template <class V> __device__ __forceinline__ V times_minus_one(V v) { return v * (V)-1; }
+
 // .x of a read: uint for unsigned pixels, int for signed, float for float
 template <class S> __device__ __forceinline__ auto readx(const S* p, int64_t i) {
   const S t = __ldg(p + i);
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(kBlock)
       for (int ay = -1; ay <= 1; ++ay)
         for (int az = -1; az <= 1; ++az) {
           const auto v = readx(src, atc(sd, x + ax, y + ay, z + az));
-          result = __fadd_rn(result, (ax == 0 && ay == 0 && az == 0) ? (float)v : (float)(v * -1));
+          result = __fadd_rn(result, (ax == 0 && ay == 0 && az == 0) ? (float)v : (float)times_minus_one(v));
         }
     dst[at(dd, x, y, z)] = convert_sat<D>(result, rte);
   }
@@ -265,7 +269,7 @@ __global__ void __launch_bounds__(256)
       const int i = tid + k * 256;
       if (i < NS) {
         const int r = i / (LBX + 2), c = i - r * (LBX + 2);
-        t[r * LBP + c] = (float)(pre[k] * -1);
+        t[r * LBP + c] = (float)times_minus_one(pre[k]);
       }
     }
   };
