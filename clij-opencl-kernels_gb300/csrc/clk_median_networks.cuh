@@ -243,8 +243,41 @@ template <class V> CLK_NET_FN void net_merge99_r1_16_raw(V (&w)[18]) {
 CLK_NET_CONST int net_merge99_r1_16_out[16] = {1, 2, 3, 4, 5, 6, 7, 8, 10, 11, 12, 13, 14, 15, 16, 9};
 
 // sorted 16 w[0..15] U sorted 9 w[16..24] U 6 singles -> rank 15
-// 104 min/max operations
+// 84 min/max operations
 template <class V> CLK_NET_FN void net_sphere33_pair_final_raw(V (&w)[31]) {
+  w[16] = vmax(w[0], w[16]);
+  w[8] = vmin(w[8], w[24]);
+  w[16] = vmax(w[8], w[16]);
+  w[20] = vmax(w[4], w[20]);
+  w[12] = vmin(w[12], w[20]);
+  { const V t = vmin(w[12], w[16]); w[16] = vmax(w[12], w[16]); w[12] = t; }
+  w[18] = vmax(w[2], w[18]);
+  { const V t = vmin(w[10], w[18]); w[18] = vmax(w[10], w[18]); w[10] = t; }
+  { const V t = vmin(w[6], w[22]); w[22] = vmax(w[6], w[22]); w[6] = t; }
+  w[14] = vmin(w[14], w[22]);
+  w[10] = vmax(w[6], w[10]);
+  w[14] = vmin(w[14], w[18]);
+  { const V t = vmin(w[10], w[12]); w[12] = vmax(w[10], w[12]); w[10] = t; }
+  { const V t = vmin(w[14], w[16]); w[16] = vmax(w[14], w[16]); w[14] = t; }
+  w[17] = vmax(w[1], w[17]);
+  { const V t = vmin(w[9], w[17]); w[17] = vmax(w[9], w[17]); w[9] = t; }
+  { const V t = vmin(w[5], w[21]); w[21] = vmax(w[5], w[21]); w[5] = t; }
+  w[13] = vmin(w[13], w[21]);
+  w[9] = vmax(w[5], w[9]);
+  { const V t = vmin(w[13], w[17]); w[17] = vmax(w[13], w[17]); w[13] = t; }
+  w[19] = vmax(w[3], w[19]);
+  { const V t = vmin(w[11], w[19]); w[19] = vmax(w[11], w[19]); w[11] = t; }
+  { const V t = vmin(w[7], w[23]); w[23] = vmax(w[7], w[23]); w[7] = t; }
+  w[15] = vmin(w[15], w[23]);
+  { const V t = vmin(w[7], w[11]); w[11] = vmax(w[7], w[11]); w[7] = t; }
+  w[15] = vmin(w[15], w[19]);
+  w[9] = vmax(w[7], w[9]);
+  { const V t = vmin(w[11], w[13]); w[13] = vmax(w[11], w[13]); w[11] = t; }
+  w[15] = vmin(w[15], w[17]);
+  { const V t = vmin(w[9], w[10]); w[10] = vmax(w[9], w[10]); w[9] = t; }
+  { const V t = vmin(w[11], w[12]); w[12] = vmax(w[11], w[12]); w[11] = t; }
+  { const V t = vmin(w[13], w[14]); w[14] = vmax(w[13], w[14]); w[13] = t; }
+  w[15] = vmin(w[15], w[16]);
   { const V t = vmin(w[25], w[26]); w[26] = vmax(w[25], w[26]); w[25] = t; }
   { const V t = vmin(w[27], w[28]); w[28] = vmax(w[27], w[28]); w[27] = t; }
   { const V t = vmin(w[25], w[27]); w[27] = vmax(w[25], w[27]); w[25] = t; }
@@ -257,61 +290,18 @@ template <class V> CLK_NET_FN void net_sphere33_pair_final_raw(V (&w)[31]) {
   { const V t = vmin(w[28], w[30]); w[30] = vmax(w[28], w[30]); w[28] = t; }
   { const V t = vmin(w[26], w[27]); w[27] = vmax(w[26], w[27]); w[26] = t; }
   { const V t = vmin(w[28], w[29]); w[29] = vmax(w[28], w[29]); w[28] = t; }
-  { const V t = vmin(w[16], w[25]); w[25] = vmax(w[16], w[25]); w[16] = t; }
-  { const V t = vmin(w[24], w[25]); w[25] = vmax(w[24], w[25]); w[24] = t; }
-  { const V t = vmin(w[20], w[29]); w[29] = vmax(w[20], w[29]); w[20] = t; }
-  { const V t = vmin(w[20], w[24]); w[24] = vmax(w[20], w[24]); w[20] = t; }
-  { const V t = vmin(w[29], w[25]); w[25] = vmax(w[29], w[25]); w[29] = t; }
-  { const V t = vmin(w[18], w[27]); w[27] = vmax(w[18], w[27]); w[18] = t; }
-  { const V t = vmin(w[22], w[27]); w[27] = vmax(w[22], w[27]); w[22] = t; }
-  { const V t = vmin(w[18], w[20]); w[20] = vmax(w[18], w[20]); w[18] = t; }
-  { const V t = vmin(w[22], w[24]); w[24] = vmax(w[22], w[24]); w[22] = t; }
-  { const V t = vmin(w[27], w[29]); w[29] = vmax(w[27], w[29]); w[27] = t; }
-  { const V t = vmin(w[17], w[26]); w[26] = vmax(w[17], w[26]); w[17] = t; }
-  { const V t = vmin(w[21], w[30]); w[30] = vmax(w[21], w[30]); w[21] = t; }
-  { const V t = vmin(w[21], w[26]); w[26] = vmax(w[21], w[26]); w[21] = t; }
-  { const V t = vmin(w[19], w[28]); w[28] = vmax(w[19], w[28]); w[19] = t; }
-  { const V t = vmin(w[23], w[28]); w[28] = vmax(w[23], w[28]); w[23] = t; }
-  { const V t = vmin(w[19], w[21]); w[21] = vmax(w[19], w[21]); w[19] = t; }
-  { const V t = vmin(w[23], w[26]); w[26] = vmax(w[23], w[26]); w[23] = t; }
-  { const V t = vmin(w[28], w[30]); w[30] = vmax(w[28], w[30]); w[28] = t; }
-  { const V t = vmin(w[17], w[18]); w[18] = vmax(w[17], w[18]); w[17] = t; }
-  { const V t = vmin(w[19], w[20]); w[20] = vmax(w[19], w[20]); w[19] = t; }
-  { const V t = vmin(w[21], w[22]); w[22] = vmax(w[21], w[22]); w[21] = t; }
-  { const V t = vmin(w[23], w[24]); w[24] = vmax(w[23], w[24]); w[23] = t; }
-  { const V t = vmin(w[26], w[27]); w[27] = vmax(w[26], w[27]); w[26] = t; }
-  { const V t = vmin(w[28], w[29]); w[29] = vmax(w[28], w[29]); w[28] = t; }
-  { const V t = vmin(w[30], w[25]); w[25] = vmax(w[30], w[25]); w[30] = t; }
-  w[16] = vmax(w[0], w[16]);
-  w[8] = vmin(w[8], w[24]);
-  w[16] = vmax(w[8], w[16]);
-  w[20] = vmax(w[4], w[20]);
-  w[12] = vmin(w[12], w[29]);
-  w[12] = vmin(w[12], w[20]);
-  w[16] = vmax(w[12], w[16]);
-  w[18] = vmax(w[2], w[18]);
-  w[10] = vmin(w[10], w[27]);
-  w[18] = vmax(w[10], w[18]);
-  w[22] = vmax(w[6], w[22]);
-  w[14] = vmin(w[14], w[25]);
-  w[14] = vmin(w[14], w[22]);
-  w[14] = vmin(w[14], w[18]);
-  w[16] = vmax(w[14], w[16]);
-  w[17] = vmax(w[1], w[17]);
-  w[9] = vmin(w[9], w[26]);
-  w[17] = vmax(w[9], w[17]);
-  w[21] = vmax(w[5], w[21]);
-  w[13] = vmin(w[13], w[30]);
-  w[13] = vmin(w[13], w[21]);
-  w[17] = vmax(w[13], w[17]);
-  w[19] = vmax(w[3], w[19]);
-  w[11] = vmin(w[11], w[28]);
-  w[19] = vmax(w[11], w[19]);
-  w[23] = vmax(w[7], w[23]);
-  w[15] = vmin(w[15], w[23]);
-  w[15] = vmin(w[15], w[19]);
-  w[15] = vmin(w[15], w[17]);
-  w[15] = vmin(w[15], w[16]);
+  w[14] = vmax(w[25], w[14]);
+  w[13] = vmax(w[26], w[13]);
+  w[12] = vmax(w[27], w[12]);
+  w[11] = vmax(w[28], w[11]);
+  w[10] = vmax(w[29], w[10]);
+  w[9] = vmax(w[30], w[9]);
+  w[15] = vmin(w[15], w[14]);
+  w[15] = vmin(w[15], w[13]);
+  w[15] = vmin(w[15], w[12]);
+  w[15] = vmin(w[15], w[11]);
+  w[15] = vmin(w[15], w[10]);
+  w[15] = vmin(w[15], w[9]);
 }
 CLK_NET_CONST int net_sphere33_pair_final_out[1] = {15};
 
