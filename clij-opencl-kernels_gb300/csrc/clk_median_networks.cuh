@@ -102,45 +102,8 @@ template <class V> CLK_NET_FN void net_box27_final_raw(V (&w)[19]) {
 CLK_NET_CONST int net_box27_final_out[1] = {9};
 
 // sorted 9 x3 + 4 + 2 singles -> rank 16
-// 166 min/max operations
+// 146 min/max operations
 template <class V> CLK_NET_FN void net_sphere33_final_raw(V (&w)[33]) {
-  { const V t = vmin(w[27], w[28]); w[28] = vmax(w[27], w[28]); w[27] = t; }
-  { const V t = vmin(w[29], w[30]); w[30] = vmax(w[29], w[30]); w[29] = t; }
-  { const V t = vmin(w[27], w[29]); w[29] = vmax(w[27], w[29]); w[27] = t; }
-  { const V t = vmin(w[28], w[30]); w[30] = vmax(w[28], w[30]); w[28] = t; }
-  { const V t = vmin(w[28], w[29]); w[29] = vmax(w[28], w[29]); w[28] = t; }
-  { const V t = vmin(w[31], w[32]); w[32] = vmax(w[31], w[32]); w[31] = t; }
-  { const V t = vmin(w[27], w[31]); w[31] = vmax(w[27], w[31]); w[27] = t; }
-  { const V t = vmin(w[29], w[31]); w[31] = vmax(w[29], w[31]); w[29] = t; }
-  { const V t = vmin(w[28], w[32]); w[32] = vmax(w[28], w[32]); w[28] = t; }
-  { const V t = vmin(w[30], w[32]); w[32] = vmax(w[30], w[32]); w[30] = t; }
-  { const V t = vmin(w[28], w[29]); w[29] = vmax(w[28], w[29]); w[28] = t; }
-  { const V t = vmin(w[30], w[31]); w[31] = vmax(w[30], w[31]); w[30] = t; }
-  { const V t = vmin(w[18], w[27]); w[27] = vmax(w[18], w[27]); w[18] = t; }
-  { const V t = vmin(w[26], w[27]); w[27] = vmax(w[26], w[27]); w[26] = t; }
-  { const V t = vmin(w[22], w[31]); w[31] = vmax(w[22], w[31]); w[22] = t; }
-  { const V t = vmin(w[22], w[26]); w[26] = vmax(w[22], w[26]); w[22] = t; }
-  { const V t = vmin(w[31], w[27]); w[27] = vmax(w[31], w[27]); w[31] = t; }
-  { const V t = vmin(w[20], w[29]); w[29] = vmax(w[20], w[29]); w[20] = t; }
-  { const V t = vmin(w[24], w[29]); w[29] = vmax(w[24], w[29]); w[24] = t; }
-  { const V t = vmin(w[20], w[22]); w[22] = vmax(w[20], w[22]); w[20] = t; }
-  { const V t = vmin(w[24], w[26]); w[26] = vmax(w[24], w[26]); w[24] = t; }
-  { const V t = vmin(w[29], w[31]); w[31] = vmax(w[29], w[31]); w[29] = t; }
-  { const V t = vmin(w[19], w[28]); w[28] = vmax(w[19], w[28]); w[19] = t; }
-  { const V t = vmin(w[23], w[32]); w[32] = vmax(w[23], w[32]); w[23] = t; }
-  { const V t = vmin(w[23], w[28]); w[28] = vmax(w[23], w[28]); w[23] = t; }
-  { const V t = vmin(w[21], w[30]); w[30] = vmax(w[21], w[30]); w[21] = t; }
-  { const V t = vmin(w[25], w[30]); w[30] = vmax(w[25], w[30]); w[25] = t; }
-  { const V t = vmin(w[21], w[23]); w[23] = vmax(w[21], w[23]); w[21] = t; }
-  { const V t = vmin(w[25], w[28]); w[28] = vmax(w[25], w[28]); w[25] = t; }
-  { const V t = vmin(w[30], w[32]); w[32] = vmax(w[30], w[32]); w[30] = t; }
-  { const V t = vmin(w[19], w[20]); w[20] = vmax(w[19], w[20]); w[19] = t; }
-  { const V t = vmin(w[21], w[22]); w[22] = vmax(w[21], w[22]); w[21] = t; }
-  { const V t = vmin(w[23], w[24]); w[24] = vmax(w[23], w[24]); w[23] = t; }
-  { const V t = vmin(w[25], w[26]); w[26] = vmax(w[25], w[26]); w[25] = t; }
-  { const V t = vmin(w[28], w[29]); w[29] = vmax(w[28], w[29]); w[28] = t; }
-  { const V t = vmin(w[30], w[31]); w[31] = vmax(w[30], w[31]); w[30] = t; }
-  { const V t = vmin(w[32], w[27]); w[27] = vmax(w[32], w[27]); w[32] = t; }
   { const V t = vmin(w[0], w[9]); w[9] = vmax(w[0], w[9]); w[0] = t; }
   { const V t = vmin(w[8], w[17]); w[17] = vmax(w[8], w[17]); w[8] = t; }
   { const V t = vmin(w[8], w[9]); w[9] = vmax(w[8], w[9]); w[8] = t; }
@@ -176,33 +139,60 @@ template <class V> CLK_NET_FN void net_sphere33_final_raw(V (&w)[33]) {
   w[8] = vmin(w[8], w[26]);
   w[9] = vmax(w[8], w[9]);
   w[22] = vmax(w[4], w[22]);
-  w[13] = vmin(w[13], w[31]);
   w[13] = vmin(w[13], w[22]);
-  w[9] = vmax(w[13], w[9]);
+  { const V t = vmin(w[13], w[9]); w[9] = vmax(w[13], w[9]); w[13] = t; }
   w[20] = vmax(w[2], w[20]);
-  w[11] = vmin(w[11], w[29]);
-  w[20] = vmax(w[11], w[20]);
-  w[24] = vmax(w[6], w[24]);
-  w[15] = vmin(w[15], w[27]);
+  { const V t = vmin(w[11], w[20]); w[20] = vmax(w[11], w[20]); w[11] = t; }
+  { const V t = vmin(w[6], w[24]); w[24] = vmax(w[6], w[24]); w[6] = t; }
   w[15] = vmin(w[15], w[24]);
+  w[11] = vmax(w[6], w[11]);
   w[15] = vmin(w[15], w[20]);
-  w[9] = vmax(w[15], w[9]);
+  { const V t = vmin(w[11], w[13]); w[13] = vmax(w[11], w[13]); w[11] = t; }
+  { const V t = vmin(w[15], w[9]); w[9] = vmax(w[15], w[9]); w[15] = t; }
   w[19] = vmax(w[1], w[19]);
   w[17] = vmin(w[17], w[19]);
-  w[10] = vmin(w[10], w[28]);
-  w[17] = vmax(w[10], w[17]);
-  w[23] = vmax(w[5], w[23]);
-  w[14] = vmin(w[14], w[32]);
+  { const V t = vmin(w[10], w[17]); w[17] = vmax(w[10], w[17]); w[10] = t; }
+  { const V t = vmin(w[5], w[23]); w[23] = vmax(w[5], w[23]); w[5] = t; }
   w[14] = vmin(w[14], w[23]);
-  w[17] = vmax(w[14], w[17]);
+  w[10] = vmax(w[5], w[10]);
+  { const V t = vmin(w[14], w[17]); w[17] = vmax(w[14], w[17]); w[14] = t; }
   w[21] = vmax(w[3], w[21]);
-  w[12] = vmin(w[12], w[30]);
-  w[21] = vmax(w[12], w[21]);
-  w[25] = vmax(w[7], w[25]);
+  { const V t = vmin(w[12], w[21]); w[21] = vmax(w[12], w[21]); w[12] = t; }
+  { const V t = vmin(w[7], w[25]); w[25] = vmax(w[7], w[25]); w[7] = t; }
   w[16] = vmin(w[16], w[25]);
+  { const V t = vmin(w[7], w[12]); w[12] = vmax(w[7], w[12]); w[7] = t; }
   w[16] = vmin(w[16], w[21]);
+  w[10] = vmax(w[7], w[10]);
+  { const V t = vmin(w[12], w[14]); w[14] = vmax(w[12], w[14]); w[12] = t; }
   w[16] = vmin(w[16], w[17]);
-  w[9] = vmax(w[16], w[9]);
+  w[11] = vmax(w[10], w[11]);
+  { const V t = vmin(w[12], w[13]); w[13] = vmax(w[12], w[13]); w[12] = t; }
+  { const V t = vmin(w[14], w[15]); w[15] = vmax(w[14], w[15]); w[14] = t; }
+  { const V t = vmin(w[16], w[9]); w[9] = vmax(w[16], w[9]); w[16] = t; }
+  { const V t = vmin(w[27], w[28]); w[28] = vmax(w[27], w[28]); w[27] = t; }
+  { const V t = vmin(w[29], w[30]); w[30] = vmax(w[29], w[30]); w[29] = t; }
+  { const V t = vmin(w[27], w[29]); w[29] = vmax(w[27], w[29]); w[27] = t; }
+  { const V t = vmin(w[28], w[30]); w[30] = vmax(w[28], w[30]); w[28] = t; }
+  { const V t = vmin(w[28], w[29]); w[29] = vmax(w[28], w[29]); w[28] = t; }
+  { const V t = vmin(w[31], w[32]); w[32] = vmax(w[31], w[32]); w[31] = t; }
+  { const V t = vmin(w[27], w[31]); w[31] = vmax(w[27], w[31]); w[27] = t; }
+  { const V t = vmin(w[29], w[31]); w[31] = vmax(w[29], w[31]); w[29] = t; }
+  { const V t = vmin(w[28], w[32]); w[32] = vmax(w[28], w[32]); w[28] = t; }
+  { const V t = vmin(w[30], w[32]); w[32] = vmax(w[30], w[32]); w[30] = t; }
+  { const V t = vmin(w[28], w[29]); w[29] = vmax(w[28], w[29]); w[28] = t; }
+  { const V t = vmin(w[30], w[31]); w[31] = vmax(w[30], w[31]); w[30] = t; }
+  w[16] = vmax(w[27], w[16]);
+  w[15] = vmax(w[28], w[15]);
+  w[14] = vmax(w[29], w[14]);
+  w[13] = vmax(w[30], w[13]);
+  w[12] = vmax(w[31], w[12]);
+  w[11] = vmax(w[32], w[11]);
+  w[9] = vmin(w[9], w[16]);
+  w[9] = vmin(w[9], w[15]);
+  w[9] = vmin(w[9], w[14]);
+  w[9] = vmin(w[9], w[13]);
+  w[9] = vmin(w[9], w[12]);
+  w[9] = vmin(w[9], w[11]);
 }
 CLK_NET_CONST int net_sphere33_final_out[1] = {9};
 

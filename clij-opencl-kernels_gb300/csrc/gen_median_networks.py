@@ -158,15 +158,23 @@ def main():
     parts.append(("net_box27_final_raw", 19, prog, [r[9]], "sorted 10 w[0..9] U sorted 9 w[10..18] -> rank 9"))
 
     # sphere33 final: 0-8, 9-17 sorted 9 (planes z-1, z+1); 18-26 sorted 9 (plane z);
-    # 27-30 four singles (x+-2, y+-2 in plane z); 31, 32 singles (z-2, z+2)
-    # merge tree ((A, B), (C, (F, S))): the cheapest of the shapes tried
+    # 27-30 four singles (x+-2, y+-2 in plane z); 31, 32 singles (z-2, z+2).
+    # The three sorted 9s merged for ranks 10..16 only, the six singles
+    # sorted, rank 16 of the union by C[k] = min over i of max(S[i-1],
+    # X[k-i]), i = 0..6 (146 operations against 166 for the best pruned
+    # merge tree)
+    net = []
+    x = oe_merge(oe_merge(list(range(9)), list(range(9, 18)), net), list(range(18, 27)), net)
+    prog = prune(net, [x[16 - i] for i in range(7)])
     net = []
     s4 = oe_merge(oe_merge([27], [28], net), oe_merge([29], [30], net), net)
-    s2 = oe_merge([31], [32], net)
-    q = oe_merge(list(range(18, 27)), oe_merge(s4, s2, net), net)
-    m = oe_merge(list(range(9)), list(range(9, 18)), net)
-    allr = oe_merge(m, q, net)
-    prog = prune(net, [allr[16]])
+    s6 = oe_merge(s4, oe_merge([31], [32], net), net)
+    prog += prune(net, s6)
+    for i in range(1, 7):
+        prog.append(("max", s6[i - 1], x[16 - i]))
+    for i in range(1, 7):
+        prog.append(("min", x[16], x[16 - i]))
+    allr = {16: x[16]}
     verify(prog, 33, [list(range(9)), list(range(9, 18)), list(range(18, 27))],
            lambda v, o: o[allr[16]] == sorted(v)[16], exhaustive=False, trials=200000)
     stats["sphere33_final"] = ops(prog)
