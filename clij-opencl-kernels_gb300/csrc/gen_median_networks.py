@@ -9,8 +9,11 @@ pixels (median_box_3d_x.cl:3-20 sorts and takes element n/2).  The networks
 are built from Batcher odd-even merges of already sorted lists and pruned
 backwards to the ranks that are actually consumed: a comparator whose min
 (or max) is never used becomes a single max (or min), one whose outputs are
-both unused disappears.  Every network is checked here on all 0/1 inputs
-of its sorted-input structure (0-1 principle) and on random values.
+both unused disappears; the sphere's final selections end with the identity
+for two sorted lists C[k] = min_i max(S[i-1], X[k-i]).  Every network is
+checked here on all 0/1 inputs of its sorted-input structure (0-1
+principle: exhaustively over the ones-counts of its sorted groups and every
+0/1 pattern of its free wires) and on random values.
 
 Networks (V is a SIMD word: two 16-bit lanes, one output each):
   net_sort3            sort three values (a z- or y-column)
@@ -104,6 +107,26 @@ def verify(prog, n, groups, checks, exhaustive=True, trials=20000):
         assert checks(v, run(prog, v)), v
 
 
+def verify_01_groups(prog, n, groups, rank, out_wire):
+    """Exhaustive 0-1 check of a selection network whose inputs are sorted
+    groups plus free wires: a sorted 0/1 group is fixed by its count of ones,
+    so every 0/1 input of that structure is enumerated (by the 0-1
+    principle, a min/max network that selects rank `rank` on all of them
+    selects it on every input)."""
+    grouped = {w for g in groups for w in g}
+    free = [w for w in range(n) if w not in grouped]
+    for counts in itertools.product(*[range(len(g) + 1) for g in groups]):
+        base = [0] * n
+        for g, c in zip(groups, counts):
+            for w in g[len(g) - c:]:
+                base[w] = 1
+        for bits in itertools.product((0, 1), repeat=len(free)):
+            v = list(base)
+            for w, b in zip(free, bits):
+                v[w] = b
+            assert run(prog, v)[out_wire] == sorted(v)[rank], (counts, bits)
+
+
 def emit(name, n, prog, args_doc):
     lines = [f"// {args_doc}", f"// {ops(prog)} min/max operations",
              f"template <class V> CLK_NET_FN void {name}(V (&w)[{n}]) {{"]
@@ -177,6 +200,7 @@ def main():
     allr = {16: x[16]}
     verify(prog, 33, [list(range(9)), list(range(9, 18)), list(range(18, 27))],
            lambda v, o: o[allr[16]] == sorted(v)[16], exhaustive=False, trials=200000)
+    verify_01_groups(prog, 33, [list(range(9)), list(range(9, 18)), list(range(18, 27))], 16, allr[16])
     stats["sphere33_final"] = ops(prog)
     parts.append(("net_sphere33_final_raw", 33, prog, [allr[16]], "sorted 9 x3 + 4 + 2 singles -> rank 16"))
 
@@ -214,6 +238,7 @@ def main():
     allr = {15: ab[15]}
     verify(prog, 31, [list(range(16)), list(range(16, 25))],
            lambda v, o: o[allr[15]] == sorted(v)[15], exhaustive=False, trials=200000)
+    verify_01_groups(prog, 31, [list(range(16)), list(range(16, 25))], 15, allr[15])
     stats["sphere33_pair_final"] = ops(prog)
     parts.append(("net_sphere33_pair_final_raw", 31, prog, [allr[15]],
                   "sorted 16 w[0..15] U sorted 9 w[16..24] U 6 singles -> rank 15"))
