@@ -31,6 +31,8 @@ clk_status fail(clk_status st, const char* fmt, ...) {
   return st;
 }
 
+void clear_error() { t_error.clear(); }
+
 clk_status check_launch(const char* what) {
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(CLK_LAUNCH_FAILED, "%s: %s", what, cudaGetErrorString(e));
@@ -214,15 +216,28 @@ const KernelInfo* find_kernel(const char* name) {
 volatile int* g_wait_flag_host = nullptr;
 int* g_wait_flag_dev = nullptr;
 
-clk_status device_ready() {
+std::once_flag g_wait_flag_once;
+
+// CLK_OK if a device exists; reports (and clears) a wait that ran out in an
+// earlier launch once the wait flag is mapped.
+clk_status device_present() {
   static int count = -1;
-  static std::once_flag mapped;
   if (count < 0) {
     if (cudaGetDeviceCount(&count) != cudaSuccess) count = 0;
     cudaGetLastError();
   }
   if (count <= 0) return fail(CLK_NO_DEVICE, "no CUDA device available");
-  std::call_once(mapped, [] {
+  if (g_wait_flag_host && *g_wait_flag_host) {
+    *g_wait_flag_host = 0;
+    return fail(CLK_TIMEOUT, "a bounded wait for a staged tile ran out in an earlier launch; its output is incomplete");
+  }
+  return CLK_OK;
+}
+
+clk_status device_ready() {
+  clk_status st = device_present();
+  if (st) return st;
+  std::call_once(g_wait_flag_once, [] {
     void* h = nullptr;
     void* d = nullptr;
     if (cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable) == cudaSuccess &&
@@ -233,10 +248,6 @@ clk_status device_ready() {
     }
     cudaGetLastError();
   });
-  if (g_wait_flag_host && *g_wait_flag_host) {
-    *g_wait_flag_host = 0;
-    return fail(CLK_TIMEOUT, "a bounded wait for a staged tile ran out in an earlier launch; its output is incomplete");
-  }
   return CLK_OK;
 }
 
@@ -318,6 +329,7 @@ int slot_of(const KernelInfo& k, const char* nm) {
 }  // namespace
 
 clk_status device_ready_public() { return device_ready(); }
+clk_status device_ready_no_alloc() { return device_present(); }
 
 clk_status sep_pass(SepOp op, const Image& dst, const Image& src, int axis, const SepTaps& taps, Range r,
                     const Policy& pol, cudaStream_t st) {
@@ -330,7 +342,7 @@ int* wait_flag_device() { return g_wait_flag_dev; }
 
 clk_status separable_plan(const char* kernel_name, const clk_image* dst_img, const clk_image* src_img,
                           const int32_t N[3], const float s[3], const clk_define* defines, size_t ndefines,
-                          SepPlan* plan) {
+                          SepPlan* plan, bool may_allocate) {
   const KernelInfo* k = find_kernel(kernel_name);
   if (!k) return fail(CLK_UNKNOWN_KERNEL, "unknown kernel '%s'", kernel_name ? kernel_name : "(null)");
   if (k->fam != F_SEP) return fail(CLK_BAD_ARG, "%s is not a separable kernel", k->name);
@@ -355,7 +367,7 @@ clk_status separable_plan(const char* kernel_name, const clk_image* dst_img, con
       box_taps(N[d], &plan->taps[d]);
     }
   }
-  return device_ready();
+  return may_allocate ? device_ready() : device_present();
 }
 
 }  // namespace clk

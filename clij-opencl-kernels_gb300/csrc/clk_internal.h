@@ -62,10 +62,15 @@ struct MedianNbhd {
 
 // error reporting (thread-local message) and launch accounting
 clk_status fail(clk_status st, const char* fmt, ...);
+void clear_error();  // empty the calling thread's message (start of every entry point)
 clk_status check_launch(const char* what);
 void count_launch(int n = 1);
 void uncount_launches(uint64_t n);  // launches recorded while capturing a graph
 clk_status device_ready_public();   // CLK_NO_DEVICE (with message) if no GPU
+// The same check without the one-time mapping of the wait flag (a pinned host
+// allocation): for the entry point that must allocate nothing.  Until some
+// other call has mapped the flag, kernels that need it are not chosen.
+clk_status device_ready_no_alloc();
 // Device pointer of a host-mapped word that kernels set to 1 when one of
 // their bounded waits runs out (nullptr if it could not be mapped).  The next
 // entry-point call reports that as CLK_TIMEOUT and clears the word.
@@ -91,7 +96,8 @@ struct SepPlan {
   SepTaps taps[3];
 };
 clk_status separable_plan(const char* kernel_name, const clk_image* dst, const clk_image* src, const int32_t N[3],
-                          const float s[3], const clk_define* defines, size_t ndefines, SepPlan* plan);
+                          const float s[3], const clk_define* defines, size_t ndefines, SepPlan* plan,
+                          bool may_allocate = true);
 
 // ---- generic ("direct") kernels: one thread per output voxel, every
 // pixel-type pair, the reference's own evaluation order (bit-exact).

@@ -159,19 +159,22 @@ clk_status clk_separable(const char* kernel_name, const clk_image* dst,
                          size_t ndefines, void* stream);
 
 /* ---------------------------------------------------------------------
- * clk_separable for callers that cannot let the library allocate device
- * memory: a host application that owns the whole device-memory budget and
- * forbids allocations it does not make itself, a loop that must not stall
- * or fail with out-of-memory halfway through, or a plugin whose host
- * manages all GPU memory.  This entry point has no counterpart in the
- * reference.
- * Same arguments, results and errors as clk_separable, computed pass by
- * pass; the two temporaries come from one fixed array in device memory
- * (64 MiB, held by every GPU that loads the library until the process
- * exits), so a call allocates nothing.  Limit: dst voxels x dst pixel size
- * must be at most 32 MiB, else CLK_BAD_ARG.  The first call on each device
- * looks up the array's device address (make it outside any stream
- * capture).  Calls share the array: calls that overlap on the GPU race.
+ * clk_separable for callers that cannot let the library allocate memory:
+ * a host application that owns the whole device-memory budget and forbids
+ * allocations it does not make itself, a loop that must not stall or fail
+ * with out-of-memory halfway through, or a plugin whose host manages all
+ * GPU memory.  This entry point has no counterpart in the reference.
+ * Same arguments, errors and results as clk_separable, bit for bit: it
+ * runs the same fused kernel where one applies (no temporaries at all), and
+ * otherwise the same passes, with the two temporaries in one fixed array in
+ * device memory (64 MiB, held by every GPU that loads the library until the
+ * process exits) instead of the stream-ordered allocator.  A call allocates
+ * nothing: no device memory, and not the pinned host word the other entry
+ * points map on their first call.  Limit, for the pass-by-pass form only:
+ * dst voxels x dst pixel size at most 32 MiB, else CLK_BAD_ARG.  The first
+ * call in each CUDA context looks up the array's device address (make it
+ * outside any stream capture).  Calls share the array: calls that overlap
+ * on the GPU race.
  * ------------------------------------------------------------------- */
 clk_status clk_separable_noalloc(const char* kernel_name, const clk_image* dst,
                                  const clk_image* src, const int32_t N[3],

@@ -37,7 +37,15 @@ HERE = Path(__file__).resolve().parent
 REF_DIR = HERE / "_ref"
 GEN_DIR = REF_DIR / "gen"
 LIB = REF_DIR / "libclkref.so"
-DEFAULT_REFERENCE = Path("/root/reference")
+# The reference checkout: the argument of build() / generate(), else the
+# environment variable CLK_REFERENCE_DIR.  There is no default location.
+REFERENCE_ENV = "CLK_REFERENCE_DIR"
+
+
+def reference_dir(reference: Path | str | None = None) -> Path | None:
+    if reference is None:
+        reference = os.environ.get(REFERENCE_ENV) or None
+    return Path(reference) if reference else None
 
 KERNELS = [
     "gaussian_blur_separable_2d", "gaussian_blur_separable_3d",
@@ -102,7 +110,10 @@ def _params(text: str, name: str):
     return params
 
 
-def generate(reference: Path = DEFAULT_REFERENCE) -> list[Path]:
+def generate(reference: Path | str | None = None) -> list[Path]:
+    reference = reference_dir(reference)
+    if reference is None:
+        raise RuntimeError(f"no reference checkout: pass its path or set {REFERENCE_ENV}")
     GEN_DIR.mkdir(parents=True, exist_ok=True)
     files = []
     for k in KERNELS:
@@ -177,10 +188,12 @@ def compile(jobs: int | None = None, cxx: str = "g++") -> Path:
     return LIB
 
 
-def build(reference: Path = DEFAULT_REFERENCE) -> Path | None:
-    """Generate (when the reference is present) and compile; None if neither
-    the reference nor previously generated sources are available."""
-    if (reference / "kernels").is_dir():
+def build(reference: Path | str | None = None) -> Path | None:
+    """Generate (when a reference checkout is given and present) and compile;
+    None if neither the reference nor previously generated sources are
+    available."""
+    reference = reference_dir(reference)
+    if reference is not None and (reference / "kernels").is_dir():
         generate(reference)
     if not any(GEN_DIR.glob("*.cpp")):
         return None
@@ -188,5 +201,4 @@ def build(reference: Path = DEFAULT_REFERENCE) -> Path | None:
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else DEFAULT_REFERENCE
-    print(build(ref))
+    print(build(sys.argv[1] if len(sys.argv) > 1 else None))

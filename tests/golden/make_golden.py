@@ -7,7 +7,7 @@ kernel, several pixel-type pairs, border-heavy extents and parameters.  The
 committed file lets the oracle and the CUDA library be checked against the
 reference where the reference checkout is absent.
 
-    python oracle/build_ref.py && python tests/golden/make_golden.py
+    python oracle/build_ref.py <reference checkout> && python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
