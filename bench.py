@@ -10,12 +10,24 @@ value = voxels filtered per second over the whole suite (Gvoxel/s);
 per_filter gives each filter's Gvoxel/s and fraction of the measured HBM
 peak (algorithmic bytes = sizeof(src) + sizeof(dst) per voxel).
 
+The same line carries the other workloads of the benchmark, each with its
+own clocks and roofline fraction (single-GPU runs):
+  config1  plain gaussian sigma (2,2,1) on a 256x256x64 uint16 stack to f32,
+           beside the reference kernels on the host cores on the same stack;
+  batch    the top-hat chain over 512 uneven images: batched (one graph
+           launch) against per-image plain calls and per-kernel launches;
+  serve    Poisson-arrival requests at 200/1000/5000 req/s, served with
+           continuous admission against one slot, p50/p99 latency, plus a
+           closed-loop saturation run;
+  large    large-halo filters on a 2048x2048x400 float32 stack.
+
   python bench.py [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the reference kernels on the host cores (oracle/_ref:
 the reference's .cl compiled as C++, else the oracle restatement) on a
-bounded sample of the same workload.  Under torchrun each rank runs an
-independent replica (the path shards by stack; no collective).
+bounded sample of the same workload (a full-width 1024x1024x32 slab of the
+stack) and on the whole 256x256x64 stack of config1.  Under torchrun each
+rank runs an independent replica (the path shards by stack; no collective).
 """
 from __future__ import annotations
 
@@ -36,19 +48,23 @@ for p in (ROOT, ROOT / "clij-opencl-kernels_gb300"):
 SHAPE = (256, 1024, 1024)  # (z, y, x)
 N_BLOBS = 20000
 SEED = 2
-SAMPLE = (32, 256, 256)  # CPU-baseline sample: a sub-stack of the same data
+SAMPLE = (32, 1024, 1024)  # CPU-baseline sample: a full-width z-slab of the same stack
 METRIC = "Gvoxel/s (plain filter suite, 1024x1024x256)"
+CONFIG1_SHAPE, CONFIG1_BLOBS, CONFIG1_SEED = (64, 256, 256), 200, 1
+L2_FLUSH_BYTES = 512 << 20  # written between timed calls whose data fits in L2 (129 MB)
 
 
-# DRAM bytes per voxel (read + write) of each filter's kernel from the ncu
-# capture summarised in profiles/sep2_sobel_median_kernels_1024x1024x128_u16.md
-# (a 1024x1024x128 slab of the same stack; traffic scales with the voxels).
+# DRAM bytes per voxel (read + write) of each filter's kernel, from one-kernel
+# ncu captures (dram__bytes_read.sum + dram__bytes_write.sum) of the build
+# named in TRAFFIC_SOURCE, on a 1024x1024x128 slab of the same stack (traffic
+# scales with the voxels).
+TRAFFIC_SOURCE = "ncu capture of the build before commit 3a9debb (earlier sphere-median network)"
 NCU_DRAM_BYTES_PER_VOXEL = {
     "gaussian_blur s(3,3,1.5)": 5.86, "mean_box r(5,5,2)": 3.90, "minimum_box r(5,5,2)": 3.97,
     "median_box r1": 3.73, "median_sphere r2": 3.73, "sobel_3d": 5.66,
 }
 # The selection networks are bound by the min/max (ALU) pipe, not by DRAM:
-# its busy fraction from the same capture.
+# its busy fraction from the same captures.
 NCU_ALU_PIPE_BUSY = {"median_box r1": 0.80, "median_sphere r2": 0.78}
 
 
@@ -165,6 +181,34 @@ def replicas_value(local_ms: float, voxels_per_step: int, steps: int, ws: int, d
     return ms, ws * voxels_per_step * steps / (ms * 1e-3) / 1e9
 
 
+def config1_stack(device):
+    """The 256x256x64 uint16 stack of config1 (200 blobs, seed 1)."""
+    import torch
+
+    from clk import synth
+    return synth.blobs(CONFIG1_SHAPE, CONFIG1_BLOBS, seed=CONFIG1_SEED, dtype=torch.uint16, device=device)
+
+
+def reference_config1(a_np, steps: int, nt: int, kind: str):
+    """The reference kernels on the whole config1 stack (three launches of
+    gaussian_blur_separable_3d with float temporaries), best and mean of
+    `steps` runs on `nt` host threads."""
+    import numpy as np
+
+    from oracle import oracle
+    impl = "ref" if kind == "reference" else "port"
+    runs = []
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        oracle.separable("gaussian_blur_separable_3d", a_np, np.float32, (13, 13, 7), (2.0, 2.0, 1.0), impl=impl,
+                         nthreads=nt)
+        runs.append(time.perf_counter() - t0)
+    ms = statistics.mean(runs) * 1e3
+    return {"ms": round(ms, 3), "ms_best": round(min(runs) * 1e3, 3), "gvox_s": round(a_np.size / (ms * 1e-3) / 1e9, 4),
+            "cores": nt, "kind": kind, "runs": len(runs),
+            "what": "reference kernels on the host cores, the whole 256x256x64 stack"}
+
+
 def run_reference(args):
     """The reference kernels on the host cores, on a bounded sample."""
     ws, rank, _ = dist()
@@ -177,31 +221,27 @@ def run_reference(args):
     from oracle import oracle
 
     kind = "reference" if oracle.ref_available() else "port"
-    img = synth.blobs(SHAPE, N_BLOBS, seed=SEED, device="cpu") if args.full_sample else None
-    if img is None:  # same generator, restricted to the sample's extent and blob density
-        vol = SAMPLE[0] * SAMPLE[1] * SAMPLE[2]
-        nb = max(1, int(N_BLOBS * vol / (SHAPE[0] * SHAPE[1] * SHAPE[2])))
-        img = synth.blobs(SAMPLE, nb, seed=SEED, device="cpu")
-    a = img[:SAMPLE[0], :SAMPLE[1], :SAMPLE[2]].contiguous().numpy()
+    # a full-width slab of the stack's extent with the stack's blob density
+    nb = max(1, int(N_BLOBS * SAMPLE[0] / SHAPE[0]))
+    img = synth.blobs(SAMPLE, nb, seed=SEED, device="cpu")
+    a = img.contiguous().numpy()
     mask = (a > 400).astype(np.uint8)
     nt = os.cpu_count() or 1
     spec = suite_spec()
     NP = {0: np.uint8, 2: np.uint16, 4: np.float32}
+    impl = "ref" if kind == "reference" else "port"
 
     def one_step():
         for name, kindf, kernel, params, srcn, ddt, bpv in spec:
             src = a if srcn == "img" else mask
             if kindf == "sep":
-                oracle.separable(kernel, src, NP[ddt], params[0], params[1], impl="ref" if kind == "reference"
-                                 else "port", nthreads=nt)
+                oracle.separable(kernel, src, NP[ddt], params[0], params[1], impl=impl, nthreads=nt)
             elif kindf == "exec":
-                oracle.execute(kernel, src, NP[ddt], list(params.values()), impl="ref" if kind == "reference"
-                               else "port", nthreads=nt)
+                oracle.execute(kernel, src, NP[ddt], list(params.values()), impl=impl, nthreads=nt)
             else:
                 cur = src
                 for _ in range(params):
-                    cur = oracle.execute(kernel, cur, np.uint8, impl="ref" if kind == "reference" else "port",
-                                         nthreads=nt)
+                    cur = oracle.execute(kernel, cur, np.uint8, impl=impl, nthreads=nt)
 
     for _ in range(args.warmup):
         one_step()
@@ -211,15 +251,18 @@ def run_reference(args):
     dt = time.perf_counter() - t0
     vox = a.size * len(spec) * args.steps
     v = vox / dt / 1e9
+    c1 = reference_config1(config1_stack("cpu").numpy(), max(3, args.steps), nt, kind)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gvoxel/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16/u8 in; u16/f32/u8 out",
             "data": "synthetic (seeded blob generator)",
-            "config": {"workload": "plain filter suite on a 256x256x32 sample of the 1024x1024x256 u16 stack",
+            "config": {"workload": "plain filter suite on a 1024x1024x32 slab with the blob density of the "
+                                   "1024x1024x256 u16 stack",
                        "filters": [s[0] for s in spec]},
             "cpu_baseline": {"value": v, "unit": "Gvoxel/s", "cores": nt, "kind": kind,
                              "sample": f"{SAMPLE[2]}x{SAMPLE[1]}x{SAMPLE[0]} voxels x {len(spec)} filters"},
-            "e2e": {"value": v, "unit": "Gvoxel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": "Gvoxel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "config1": c1}
     print(json.dumps(line))
 
 
@@ -249,14 +292,37 @@ def batch_images(n=512, seed=3, device="cuda"):
     return imgs
 
 
-def run_batch(args):
+def event_timer(stream, steps: int, warmup: int):
+    """fn -> (mean ms per call over `steps`, per-call ms) with CUDA events on
+    `stream` after `warmup` untimed calls."""
+    import torch
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        lat = []
+        e0.record(stream)
+        for _ in range(steps):
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            z.record(stream)
+            lat.append((a, z))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, [a.elapsed_time(z) for a, z in lat]
+    return timed
+
+
+def batch_section(args, peak: float, local: int = 0):
     """Top-hat chain over 512 uneven images, batched (one graph launch)
-    against per-image plain calls, same results."""
+    against per-image plain calls and per-kernel launches, same results."""
     import torch
 
     import clk
 
-    torch.cuda.set_device(0)
     imgs = batch_images()
     outs = [torch.empty_like(t) for t in imgs]
     ops = [clk.op_separable("gaussian_blur_separable", (13, 13, 13), (2.0, 2.0, 2.0)),
@@ -267,59 +333,62 @@ def run_batch(args):
     b = clk.Batch(ops, imgs, outs)
     plan_s = time.perf_counter() - t0
     vox = sum(t.numel() for t in imgs) * len(ops)
+    nbytes = sum(2 * t.numel() * t.element_size() for t in imgs) * len(ops)  # each step reads + writes its image
     stream = torch.cuda.current_stream()
-
-    def timed(fn):
-        for _ in range(max(3, args.warmup)):
-            fn()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        lat = []
-        e0.record(stream)
-        for _ in range(args.steps):
-            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            fn()
-            z.record(stream)
-            lat.append((a, z))
-        e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / args.steps, [a.elapsed_time(z) for a, z in lat]
-
-    l0 = clk.launch_count()
-    ms_b, _ = timed(b.run)
-    launches_b = (clk.launch_count() - l0) // (args.steps + max(3, args.warmup))
+    warm = max(3, args.warmup)
+    timed = event_timer(stream, args.steps, warm)
+    with Clocks(local) as clocks:
+        l0 = clk.launch_count()
+        ms_b, lat_b = timed(b.run)
+        launches_b = (clk.launch_count() - l0) // (args.steps + warm)
     batched = [t.clone() for t in outs]
     l0 = clk.launch_count()
     ms_p, _ = timed(b.run_plain)
-    launches_p = (clk.launch_count() - l0) // (args.steps + max(3, args.warmup))
+    launches_p = (clk.launch_count() - l0) // (args.steps + warm)
     same = all(torch.equal(x.view(torch.uint8) if x.dtype != torch.uint8 else x,
                            y.view(torch.uint8) if y.dtype != torch.uint8 else y) for x, y in zip(batched, outs))
     l0 = clk.launch_count()
     ms_k, _ = timed(b.run_per_kernel)
-    launches_k = (clk.launch_count() - l0) // (args.steps + max(3, args.warmup))
+    launches_k = (clk.launch_count() - l0) // (args.steps + warm)
     n_u8 = sum(t.dtype == torch.uint8 for t in imgs)
     n_u16 = sum(t.dtype == torch.uint16 for t in imgs)
-    line = {
-        "metric": "Gvoxel/s (batched pipeline, 512 uneven images)", "value": round(vox / (ms_b * 1e-3) / 1e9, 3),
-        "unit": "Gvoxel/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
-        "ms_per_step": round(ms_b, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u8/u16/f32 pixels, same type out", "data": "synthetic: seeded blob images, intensities scaled to type",
-        "config": {"workload": "batched top-hat: 512 images (half 2-D XY in [64,1024], half 3-D XY in [64,512] x Z in "
-                               "[16,128]), top-hat chain gaussian s=2 -> minimum r=4 -> maximum r=4 -> median_box r=1",
-                   "images": len(imgs), "u8": n_u8, "u16": n_u16, "f32": len(imgs) - n_u8 - n_u16,
-                   "voxels_per_step": vox, "l2": "working set far larger than L2"},
+    gbs = nbytes / (ms_b * 1e-3) / 1e9
+    res = {
+        "value": round(vox / (ms_b * 1e-3) / 1e9, 3), "unit": "Gvoxel/s", "ms_per_step": round(ms_b, 4),
+        "ms_best": round(min(lat_b), 4), "steps": args.steps, "warmup": warm,
+        "workload": "batched top-hat: 512 images (half 2-D XY in [64,1024], half 3-D XY in [64,512] x Z in "
+                    "[16,128]), gaussian s=2 -> minimum r=4 -> maximum r=4 -> median_box r=1",
+        "images": len(imgs), "u8": n_u8, "u16": n_u16, "f32": len(imgs) - n_u8 - n_u16,
+        "voxels_per_step": vox, "l2": "working set far larger than L2",
+        "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(gbs / peak, 4), "algorithmic_bytes_per_step": nbytes},
         "plain": {"value": round(vox / (ms_p * 1e-3) / 1e9, 3), "ms_per_step": round(ms_p, 4),
                   "launches_per_step": launches_p, "what": "per image, whole-filter calls (clk_separable, "
                                                            "clk_execute), one stream"},
         "per_kernel": {"value": round(vox / (ms_k * 1e-3) / 1e9, 3), "ms_per_step": round(ms_k, 4),
                        "launches_per_step": launches_k, "what": "per image, one clk_execute per kernel and axis "
                                                                 "(the reference's launch pattern)"},
-        "speedup_vs_plain": round(ms_p / ms_b, 3), "speedup_vs_per_kernel": round(ms_k / ms_b, 3), "gpu_launches": launches_b, "graph_kernels": b.launches,
-        "identical_to_plain": bool(same), "plan_and_autotune_s": round(plan_s, 2),
+        "speedup_vs_plain": round(ms_p / ms_b, 3), "speedup_vs_per_kernel": round(ms_k / ms_b, 3),
+        "gpu_launches": launches_b, "graph_kernels": b.launches,
+        "identical_to_plain": bool(same), "plan_and_autotune_s": round(plan_s, 2), "clocks": clocks.result,
     }
-    print(json.dumps(line))
     b.close()
+    return res
+
+
+def run_batch(args):
+    import torch
+    torch.cuda.set_device(0)
+    peak, _ = hbm_peak()
+    r = batch_section(args, peak)
+    line = {"metric": "Gvoxel/s (batched pipeline, 512 uneven images)", "value": r["value"], "unit": "Gvoxel/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": r["warmup"], "ms_per_step": r["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u8/u16/f32 pixels, same type out",
+            "data": "synthetic: seeded blob images, intensities scaled to type",
+            "config": {"workload": r["workload"], "images": r["images"], "voxels_per_step": r["voxels_per_step"],
+                       "l2": r["l2"]}, **{k: v for k, v in r.items() if k not in ("value", "ms_per_step")}}
+    print(json.dumps(line))
 
 
 def serve_pipeline(clk, rng):
@@ -346,57 +415,80 @@ def serve_pipeline(clk, rng):
     return ops
 
 
-def run_serve(args):
+def serve_section(args, local: int = 0):
     """Served pipelines: Poisson arrivals at 200 / 1000 / 5000 req/s, each
     request one stack from the batched workload's size and type mix and a
     random 1-4 step pipeline, served with continuous admission (16 slots,
-    64 GiB budget) against the same arrivals served one at a time."""
+    64 GiB budget) against the same arrivals served one at a time; then a
+    closed-loop saturation run (every request queued at once) of both."""
     import numpy as np
     import torch
 
     import clk
 
-    torch.cuda.set_device(0)
     pool = batch_images(n=96, seed=5)
     duration = 1.5
-    results = []
-    for rate in (200, 1000, 5000):
-        rng = np.random.default_rng(rate)
-        n = int(rate * duration)
-        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
-        reqs = [(serve_pipeline(clk, rng), pool[int(rng.integers(0, len(pool)))]) for _ in range(n)]
-        outs = [torch.empty_like(src) for _, src in reqs]
-        row = {"rate_req_s": rate, "requests": n}
-        for mode, slots in (("served", 16), ("serial", 1)):
-            srv = clk.Server(slots=slots, hbm_budget_bytes=64 << 30)
-            srv.wait(srv.submit(reqs[0][0], reqs[0][1], outs[0]))  # warm-up (not counted)
-            srv.close()
-            srv = clk.Server(slots=slots, hbm_budget_bytes=64 << 30)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            tickets = []
-            for k, ((ops, src), out) in enumerate(zip(reqs, outs)):
+
+    def serve(reqs, outs, slots, arrivals):
+        srv = clk.Server(slots=slots, hbm_budget_bytes=64 << 30)
+        srv.wait(srv.submit(reqs[0][0], reqs[0][1], outs[0]))  # warm-up (not counted)
+        srv.close()
+        srv = clk.Server(slots=slots, hbm_budget_bytes=64 << 30)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k, ((ops, src), out) in enumerate(zip(reqs, outs)):
+            if arrivals is not None:
                 while time.perf_counter() - t0 < arrivals[k]:
                     pass
-                tickets.append(srv.submit(ops, src, out))
-            srv.drain(600000)
-            wall = time.perf_counter() - t0
-            st = srv.stats()
-            srv.close()
-            row[mode] = {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
-                         "mean_ms": round(st["mean_ms"], 3), "gvox_s": round(st["voxel_steps"] / wall / 1e9, 3),
-                         "completed": int(st["completed"]), "failed": int(st["failed"]),
-                         "peak_temporaries_gib": round(st["bytes_peak"] / 2**30, 3), "wall_s": round(wall, 3)}
-        results.append(row)
+            srv.submit(ops, src, out)
+        srv.drain(600000)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        return {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                "mean_ms": round(st["mean_ms"], 3), "gvox_s": round(st["voxel_steps"] / wall / 1e9, 3),
+                "completed": int(st["completed"]), "failed": int(st["failed"]),
+                "peak_temporaries_gib": round(st["bytes_peak"] / 2**30, 3), "wall_s": round(wall, 3)}
+
+    results = []
+    with Clocks(local) as clocks:
+        for rate in (200, 1000, 5000):
+            rng = np.random.default_rng(rate)
+            n = int(rate * duration)
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+            reqs = [(serve_pipeline(clk, rng), pool[int(rng.integers(0, len(pool)))]) for _ in range(n)]
+            outs = [torch.empty_like(src) for _, src in reqs]
+            row = {"rate_req_s": rate, "requests": n}
+            for mode, slots in (("served", 16), ("serial", 1)):
+                row[mode] = serve(reqs, outs, slots, arrivals)
+            results.append(row)
+        # closed loop: every request queued at t = 0, so the server runs at
+        # its capacity; served against serial is the throughput gain of
+        # continuous batching over one-at-a-time plain calls
+        rng = np.random.default_rng(7)
+        n = 2000
+        reqs = [(serve_pipeline(clk, rng), pool[int(rng.integers(0, len(pool)))]) for _ in range(n)]
+        outs = [torch.empty_like(src) for _, src in reqs]
+        sat = {"requests": n, "served": serve(reqs, outs, 16, None), "serial": serve(reqs, outs, 1, None)}
+        sat["served_over_serial"] = round(sat["served"]["gvox_s"] / max(sat["serial"]["gvox_s"], 1e-12), 3)
     top = results[-1]
+    return {"value": top["served"]["p99_ms"], "unit": "ms (p99 at 5000 req/s)",
+            "workload": "served pipelines: continuous admission, 16 slots, 64 GiB budget for temporaries; serial = "
+                        "the same arrivals through 1 slot", "duration_s_per_rate": duration,
+            "rates": results, "saturation": sat, "clocks": clocks.result}
+
+
+def run_serve(args):
+    import torch
+    torch.cuda.set_device(0)
+    r = serve_section(args)
     line = {
         "metric": "served p99 latency and Gvoxel/s (Poisson arrivals, uneven u8/u16/f32 stacks, 1-4 step pipelines)",
-        "value": top["served"]["p99_ms"], "unit": "ms (p99 at 5000 req/s)", "n_gpus": 1, "steps": len(results),
+        "value": r["value"], "unit": r["unit"], "n_gpus": 1, "steps": len(r["rates"]),
         "warmup": 1, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "u8/u16/f32 pixels, same type out", "data": "synthetic: 96 seeded blob stacks, random pipelines",
-        "config": {"workload": "served pipelines: continuous admission, 16 slots, 64 GiB budget for temporaries; serial "
-                               "= the same arrivals through 1 slot", "duration_s_per_rate": duration},
-        "rates": results,
+        "config": {"workload": r["workload"], "duration_s_per_rate": r["duration_s_per_rate"]},
+        "rates": r["rates"], "saturation": r["saturation"], "clocks": r["clocks"],
     }
     print(json.dumps(line))
 
@@ -492,7 +584,7 @@ def run_neighbours(args):
                       impl="ref" if kind == "reference" else "port", nthreads=nt)
         dt = time.perf_counter() - t0
         cpu = {"value": a.size * len(spec) / dt / 1e9, "unit": "Gvoxel/s", "cores": nt, "kind": kind,
-               "sample": f"{SAMPLE[2]}x{SAMPLE[1]}x{SAMPLE[0]} corner of the stack x {len(spec)} filters, {dt:.1f} s"}
+               "sample": f"the first {SAMPLE[0]} planes ({SAMPLE[2]}x{SAMPLE[1]}x{SAMPLE[0]}) of the stack x {len(spec)} filters, {dt:.1f} s"}
     line = {
         "metric": "Gvoxel/s (neighbourhood filters either side of the path, 1024x1024x256)",
         "value": round(V * len(spec) * args.steps / (total_ms * 1e-3) / 1e9, 3), "unit": "Gvoxel/s", "n_gpus": 1,
@@ -510,7 +602,7 @@ def run_neighbours(args):
 LARGE_SHAPE = (400, 2048, 2048)  # (z, y, x): 6.71 GB of float32
 
 
-def run_large(args):
+def large_section(args, peak: float, shape=LARGE_SHAPE, filters: str = "", local: int = 0):
     """Large-halo filters on one 2048x2048x400 float32 stack (blobs plus
     N(0, 20) noise): gaussian sigma (10,10,5) (N = 61,61,31), maximum r
     (15,15,7) and median_sphere r=2, each its own call, f32 -> f32."""
@@ -519,10 +611,8 @@ def run_large(args):
     import clk
     from clk import synth
 
-    torch.cuda.set_device(0)
-    peak, peak_kind = hbm_peak()
-    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else LARGE_SHAPE
-    img = synth.blobs(shape, N_BLOBS, seed=SEED + 5, dtype=torch.float32, poisson=False, noise_sigma=20.0)
+    img = synth.blobs(shape, max(1, int(N_BLOBS * shape[0] / LARGE_SHAPE[0])), seed=SEED + 5, dtype=torch.float32,
+                      poisson=False, noise_sigma=20.0)
     V = img.numel()
     out = torch.empty_like(img)
     stream = torch.cuda.current_stream()
@@ -534,9 +624,9 @@ def run_large(args):
         ("median_sphere r2", lambda: clk.execute("median_sphere_3d", {"src": img, "dst": out, "Nx": 5, "Ny": 5,
                                                                        "Nz": 5}, stream=stream)),
     ]
-    if args.filters:
+    if filters:
         import re
-        spec = [t for t in spec if re.search(args.filters, t[0])]
+        spec = [t for t in spec if re.search(filters, t[0])]
     for _ in range(max(3, args.warmup)):
         for _, fn in spec:
             fn()
@@ -545,7 +635,7 @@ def run_large(args):
               for _ in range(args.steps)] for n, _ in spec}
     t_begin, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = clk.launch_count()
-    with Clocks(0) as clocks:
+    with Clocks(local) as clocks:
         torch.cuda.synchronize()
         t_begin.record(stream)
         for k in range(args.steps):
@@ -559,27 +649,146 @@ def run_large(args):
     total_ms = t_begin.elapsed_time(t_end)
     per = {}
     for n, _ in spec:
-        ms = statistics.mean(a.elapsed_time(b) for a, b in ev[n])
-        per[n] = {"ms": round(ms, 3), "gvox_s": round(V / (ms * 1e-3) / 1e9, 2),
+        runs = [a.elapsed_time(b) for a, b in ev[n]]
+        ms = statistics.mean(runs)
+        per[n] = {"ms": round(ms, 3), "ms_best": round(min(runs), 3), "gvox_s": round(V / (ms * 1e-3) / 1e9, 2),
                   "hbm_frac": round(V * 8 / (ms * 1e-3) / 1e9 / peak, 4), "bytes_per_voxel": 8}
     dom = max(per, key=lambda n: per[n]["ms"])
     dom_gbs = V * 8 / (per[dom]["ms"] * 1e-3) / 1e9
+    return {"value": round(V * len(spec) * args.steps / (total_ms * 1e-3) / 1e9, 3), "unit": "Gvoxel/s",
+            "ms_per_step": round(total_ms / args.steps, 3), "steps": args.steps, "warmup": max(3, args.warmup),
+            "workload": f"large-halo filters on {shape[2]}x{shape[1]}x{shape[0]} float32, each its own call",
+            "voxels": V, "l2": "inputs larger than L2 (6.7 GB); no flush", "per_filter": per,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(dom_gbs, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(dom_gbs / peak, 4), "traffic": None},
+            "gpu_launches": launches, "clocks": clocks.result}
+
+
+def run_large(args):
+    import torch
+    torch.cuda.set_device(0)
+    peak, peak_kind = hbm_peak()
+    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else LARGE_SHAPE
+    r = large_section(args, peak, shape, args.filters)
+    r["roofline"]["peak_kind"] = peak_kind
     line = {
-        "metric": "Gvoxel/s (large-halo filters, 2048x2048x400 f32)", "value": round(
-            V * len(spec) * args.steps / (total_ms * 1e-3) / 1e9, 3), "unit": "Gvoxel/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(total_ms / args.steps, 3),
+        "metric": "Gvoxel/s (large-halo filters, 2048x2048x400 f32)", "value": r["value"], "unit": "Gvoxel/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": r["warmup"], "ms_per_step": r["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded blob stack plus N(0,20) noise, float32",
-        "config": {"workload": f"large-halo filters on {shape[2]}x{shape[1]}x{shape[0]} float32, each its own call",
-                   "voxels": V,
-                   "l2": "inputs larger than L2 (6.7 GB); no flush"},
-        "per_filter": per,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(dom_gbs, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(dom_gbs / peak, 4), "peak_kind": peak_kind, "traffic": None},
-        "gpu_launches": launches, "clocks": clocks.result,
+        "config": {"workload": r["workload"], "voxels": r["voxels"], "l2": r["l2"]},
+        "per_filter": r["per_filter"], "roofline": r["roofline"], "gpu_launches": r["gpu_launches"],
+        "clocks": r["clocks"],
     }
     print(json.dumps(line))
     return 0
+
+
+def config1_section(args, peak: float, local: int = 0, cpu: bool = True):
+    """Plain gaussian_blur_separable_3d sigma (2,2,1), N = (13,13,7), on the
+    256x256x64 uint16 stack (200 blobs) to float32.  Its 24 MiB of data fit
+    in L2, so a 512 MiB buffer is written between timed calls and each call
+    is timed alone with CUDA events.  Beside it: the reference kernels on
+    the host cores on the same stack."""
+    import torch
+
+    import clk
+
+    img = config1_stack("cuda")
+    out = torch.empty(img.shape, dtype=torch.float32, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def call():
+        clk.separable("gaussian_blur_separable_3d", img, out, (13, 13, 7), (2.0, 2.0, 1.0), stream=stream)
+
+    for _ in range(max(3, args.warmup)):
+        call()
+    torch.cuda.synchronize()
+    runs = []
+    l0 = clk.launch_count()
+    with Clocks(local) as clocks:
+        for _ in range(max(10, args.steps)):
+            flush.fill_(1.0)
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            call()
+            z.record(stream)
+            runs.append((a, z))
+        torch.cuda.synchronize()
+    launches = clk.launch_count() - l0
+    ms_runs = [a.elapsed_time(z) for a, z in runs]
+    ms = statistics.mean(ms_runs)
+    V = img.numel()
+    gbs = V * 6 / (ms * 1e-3) / 1e9
+    res = {"ms": round(ms, 4), "ms_best": round(min(ms_runs), 4), "gvox_s": round(V / (ms * 1e-3) / 1e9, 2),
+           "runs": len(ms_runs), "voxels": V,
+           "workload": "plain gaussian_blur_separable_3d s(2,2,1) N(13,13,7), 256x256x64 uint16 -> float32",
+           "l2": "512 MiB written between timed calls (the stack fits in L2)",
+           "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(gbs / peak, 4), "bytes_per_voxel": 6},
+           "gpu_launches": launches, "clocks": clocks.result}
+    if cpu:
+        try:
+            from oracle import oracle
+            kind = "reference" if oracle.ref_available() else "port"
+            ref = reference_config1(img.cpu().numpy(), 3, os.cpu_count() or 1, kind)
+            res["cpu_reference"] = ref
+            res["gpu_over_cpu_reference"] = round(ref["ms"] / ms, 1)
+        except Exception as e:  # the oracle is optional infrastructure on the box
+            res["cpu_reference"] = {"kind": "unavailable", "why": str(e)}
+    return res
+
+
+def host_link(h_img, img, h_out, outs, stream, push_kernel, zero_copy, h2d_bytes, d2h_bytes, e2e_ms):
+    """The host link's own rates, measured the way the e2e run moves its
+    bytes: host->device by copy_3d kernels reading the pinned stack (or a
+    copy engine), device->host by a copy_3d kernel storing into a pinned
+    host image (or a copy engine).  bound_ms_per_step = the step's bytes at
+    those rates with the two directions overlapped (the link is full
+    duplex); frac = bound / measured."""
+    import torch
+
+    import clk
+    name = max(outs, key=lambda n: outs[n].numel() * outs[n].element_size())
+    dev_out, hst_out = outs[name], h_out[name]
+    d_img = torch.empty_like(img)
+
+    def h2d():
+        if push_kernel:
+            clk.execute("copy_3d", {"src": h_img, "dst": d_img}, stream=stream)
+        else:
+            with torch.cuda.stream(stream):
+                d_img.copy_(h_img, non_blocking=True)
+
+    def d2h():
+        if zero_copy:
+            clk.execute("copy_3d", {"src": dev_out, "dst": hst_out}, stream=stream)
+        else:
+            with torch.cuda.stream(stream):
+                hst_out.copy_(dev_out, non_blocking=True)
+
+    res = {}
+    for key, fn, nbytes in (("h2d_gbs", h2d, h_img.numel() * h_img.element_size()),
+                            ("d2h_gbs", d2h, dev_out.numel() * dev_out.element_size())):
+        fn()
+        torch.cuda.synchronize()
+        runs = []
+        for _ in range(5):
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            z.record(stream)
+            torch.cuda.synchronize()
+            runs.append(a.elapsed_time(z))
+        res[key] = round(nbytes / (min(runs) * 1e-3) / 1e9, 1)
+    del d_img
+    bound = max(h2d_bytes / (res["h2d_gbs"] * 1e9), d2h_bytes / (res["d2h_gbs"] * 1e9)) * 1e3
+    res["bound_ms_per_step"] = round(bound, 2)
+    res["frac"] = round(bound / e2e_ms, 4)
+    res["how"] = ("best of 5 single transfers of the stack (h2d) and the largest output (d2h) through the same "
+                  "mechanism the e2e step uses")
+    return res
 
 
 def cpu_baseline(a_np, mask_np):
@@ -607,7 +816,8 @@ def cpu_baseline(a_np, mask_np):
                 cur = oracle.execute(kernel, cur, np.uint8, impl=impl, nthreads=nt)
     dt = time.perf_counter() - t0
     return {"value": a.size * len(suite_spec()) / dt / 1e9, "unit": "Gvoxel/s", "cores": nt, "kind": kind,
-            "sample": f"{SAMPLE[2]}x{SAMPLE[1]}x{SAMPLE[0]} corner of the stack x {len(suite_spec())} filters, "
+            "sample": f"the first {SAMPLE[0]} planes ({SAMPLE[2]}x{SAMPLE[1]}x{SAMPLE[0]}) of the stack x "
+                      f"{len(suite_spec())} filters, "
                       f"{dt:.1f} s"}
 
 
@@ -620,6 +830,8 @@ def main():
     ap.add_argument("--full-sample", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="suite only: skip the config1 / batch / serve / large sections of the line")
     ap.add_argument("--e2e-pull", default="zero-copy", choices=["zero-copy", "copy"],
                     help="how results reach host memory in the e2e run: the filters store into pinned host "
                          "images (zero-copy) or write device images that copy engines then pull")
@@ -628,7 +840,8 @@ def main():
                          "the pinned host images (kernel) or copy-engine copies")
     ap.add_argument("--shape", default="", help="suite stack as z,y,x (default 256,1024,1024)")
     ap.add_argument("--filters", default="", help="regex selecting suite filters by name")
-    ap.add_argument("--workload", default="suite", choices=["suite", "batch", "serve", "large", "neighbours"],
+    ap.add_argument("--workload", default="suite",
+                    choices=["suite", "batch", "serve", "large", "neighbours", "config1"],
                     help="suite: plain filter suite on 1024x1024x256 u16 (default); batch: top-hat chain over 512 uneven "
                          "images; serve: Poisson-arrival requests; large: large-halo f32 "
                          "filters on 2048x2048x400; neighbours: the filters either side of the path")
@@ -643,6 +856,11 @@ def main():
         return run_neighbours(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "config1":
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(config1_section(args, hbm_peak()[0])))
+        return 0
 
     import torch
 
@@ -810,6 +1028,8 @@ def main():
         if zero_copy:  # the host images hold the filters' results
             ok = all(torch.equal(h_out[n], outs[n].cpu()) for n in outs) if args.steps > 0 else True
             e2e["host_results_match_device"] = bool(ok)
+        e2e["link"] = host_link(h_img, img, h_out, outs, cs, push_kernel, zero_copy,
+                                e2e["h2d_bytes_per_step"], e2e["d2h_bytes_per_step"], e2e["ms_per_step"])
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -818,6 +1038,20 @@ def main():
         except Exception as e:  # the oracle is optional infrastructure on the box
             cpu = {"value": None, "unit": "Gvoxel/s", "cores": os.cpu_count(), "kind": "unavailable",
                    "sample": f"oracle could not run: {e}"}
+
+    extras = {}
+    if ws == 1 and not args.no_extras and not args.shape and not args.filters:
+        del outs, tmp_mask
+        if not args.no_e2e:
+            del h_out, h_img, h_mask, d_in, d_out
+        torch.cuda.empty_cache()
+        extras["config1"] = config1_section(args, peak, local, cpu=not args.no_cpu_baseline)
+        extras["batch"] = batch_section(args, peak, local)
+        torch.cuda.empty_cache()
+        extras["serve"] = serve_section(args, local)
+        torch.cuda.empty_cache()
+        extras["large"] = large_section(args, peak, local=local)
+        torch.cuda.empty_cache()
 
     if rank == 0:
         line = {
@@ -835,6 +1069,7 @@ def main():
                          "frac_of_nominal": round(dom_gbs / NOMINAL_HBM_GBS, 4),
                          "traffic": (round(NCU_DRAM_BYTES_PER_VOXEL[dom] * V) if dom in NCU_DRAM_BYTES_PER_VOXEL
                                      else None),
+                         "traffic_source": TRAFFIC_SOURCE,
                          "algorithmic_bytes": int(V * per[dom]["bytes_per_voxel"]),
                          **({"alu_pipe_busy": NCU_ALU_PIPE_BUSY[dom],
                              "note": "selection network: bound by the min/max (ALU) pipe, not HBM"}
@@ -843,6 +1078,7 @@ def main():
             "clocks": clocks.result,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            **extras,
         }
         print(json.dumps(line))
     if ws > 1:

@@ -12,9 +12,9 @@ PKG = Path(__file__).resolve().parent.parent
 LIB_PATH = PKG / "_build" / "libclk_gb300.so"
 
 # clk_status
-OK, UNKNOWN_KERNEL, BAD_ARG, UNSUPPORTED_DTYPE, OOM, LAUNCH_FAILED, TIMEOUT, NO_DEVICE, BUSY = range(9)
+OK, UNKNOWN_KERNEL, BAD_ARG, UNSUPPORTED_DTYPE, OOM, LAUNCH_FAILED, TIMEOUT, NO_DEVICE, BUSY, CANCELLED = range(10)
 STATUS_NAMES = ["CLK_OK", "CLK_UNKNOWN_KERNEL", "CLK_BAD_ARG", "CLK_UNSUPPORTED_DTYPE", "CLK_OOM",
-                "CLK_LAUNCH_FAILED", "CLK_TIMEOUT", "CLK_NO_DEVICE", "CLK_BUSY"]
+                "CLK_LAUNCH_FAILED", "CLK_TIMEOUT", "CLK_NO_DEVICE", "CLK_BUSY", "CLK_CANCELLED"]
 # clk_dtype
 U8, I8, U16, I16, F32 = range(5)
 # clk_arg_kind
@@ -47,7 +47,7 @@ class clk_server_stats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
                 ("bytes_in_use", C.c_int64), ("bytes_peak", C.c_int64), ("inflight", C.c_int32),
                 ("queued", C.c_int32), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
-                ("voxel_steps", C.c_double), ("busy_s", C.c_double)]
+                ("voxel_steps", C.c_double), ("busy_s", C.c_double), ("cancelled", C.c_uint64)]
 
 
 class ClkError(RuntimeError):
@@ -61,7 +61,7 @@ class ClkError(RuntimeError):
 
 EXPORTS = ["clk_execute", "clk_separable", "clk_separable_noalloc", "clk_morphology", "clk_batch_create",
            "clk_batch_run", "clk_batch_run_plain", "clk_batch_run_per_kernel", "clk_batch_launches", "clk_batch_destroy", "clk_server_create",
-           "clk_server_submit", "clk_server_wait", "clk_server_drain", "clk_server_get_stats",
+           "clk_server_submit", "clk_server_wait", "clk_server_cancel", "clk_server_drain", "clk_server_get_stats",
            "clk_server_destroy", "clk_supported", "clk_last_error_string", "clk_version",
            "clk_kernel_count", "clk_kernel_name", "clk_launch_count", "clk_host_image_pointer"]
 
@@ -108,6 +108,8 @@ def load() -> C.CDLL:
     lib.clk_server_wait.restype = C.c_int
     lib.clk_server_drain.argtypes = [C.c_void_p, C.c_int32]
     lib.clk_server_drain.restype = C.c_int
+    lib.clk_server_cancel.argtypes = [C.c_void_p, C.c_uint64]
+    lib.clk_server_cancel.restype = C.c_int
     lib.clk_server_get_stats.argtypes = [C.c_void_p, C.POINTER(clk_server_stats)]
     lib.clk_server_get_stats.restype = C.c_int
     lib.clk_server_destroy.argtypes = [C.c_void_p]

@@ -416,6 +416,10 @@ class Server:
         L.check(st)
         return lat.value
 
+    def cancel(self, ticket: int):
+        """Cancel a queued request (CLK_BUSY once it runs on the device)."""
+        L.check(L.load().clk_server_cancel(self._h, ticket))
+
     def drain(self, timeout_ms: int = 600000):
         L.check(L.load().clk_server_drain(self._h, int(timeout_ms)))
 

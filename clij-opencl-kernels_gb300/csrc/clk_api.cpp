@@ -2,6 +2,7 @@
 // named arguments, the preamble/host policies, and the separable
 // orchestration.  Host code only; kernels live in the .cu files.
 #include <cuda_runtime_api.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cmath>
@@ -32,6 +33,14 @@ clk_status fail(clk_status st, const char* fmt, ...) {
 }
 
 void clear_error() { t_error.clear(); }
+
+bool alloc_failure_injected() {
+  const char* e = getenv("CLK_INJECT_ALLOC_FAILURE");
+  return e && e[0] == '1' && e[1] == 0;
+}
+
+TraceRange::TraceRange(const char* name) { nvtxRangePushA(name ? name : "clk"); }
+TraceRange::~TraceRange() { nvtxRangePop(); }
 
 clk_status check_launch(const char* what) {
   const cudaError_t e = cudaGetLastError();
@@ -379,6 +388,7 @@ extern "C" {
 clk_status clk_execute(const char* kernel_name, const clk_arg* args, size_t nargs, const size_t* global,
                        const clk_define* defines, size_t ndefines, void* stream) {
   t_error.clear();
+  TraceRange trace(kernel_name);
   const KernelInfo* k = find_kernel(kernel_name);
   if (!k) return fail(CLK_UNKNOWN_KERNEL, "unknown kernel '%s'", kernel_name ? kernel_name : "(null)");
   Bound b;
@@ -530,6 +540,7 @@ clk_status clk_separable(const char* kernel_name, const clk_image* dst_img, cons
                          const int32_t N[3], const float s[3], const clk_define* defines, size_t ndefines,
                          void* stream) {
   t_error.clear();
+  TraceRange trace(kernel_name);
   const KernelInfo* k = find_kernel(kernel_name);
   if (!k) return fail(CLK_UNKNOWN_KERNEL, "unknown kernel '%s'", kernel_name ? kernel_name : "(null)");
   if (k->fam != F_SEP) return fail(CLK_BAD_ARG, "%s is not a separable kernel", k->name);
@@ -569,7 +580,7 @@ clk_status clk_separable(const char* kernel_name, const clk_image* dst_img, cons
   int passes = 0;
   for (int d = 0; d < k->ndim; ++d) passes += 1;
   for (int i = 0; i < 2 && i < passes - 1; ++i) {
-    if (cudaMallocAsync(&tmp[i], bytes, stm) != cudaSuccess) {
+    if (alloc_failure_injected() || cudaMallocAsync(&tmp[i], bytes, stm) != cudaSuccess) {
       cudaGetLastError();
       for (int j = 0; j < i; ++j) cudaFreeAsync(tmp[j], stm);
       return fail(CLK_OOM, "%s: cannot allocate a %zu-byte temporary", k->name, bytes);
@@ -592,6 +603,7 @@ clk_status clk_separable(const char* kernel_name, const clk_image* dst_img, cons
 clk_status clk_morphology(const char* kernel_name, const clk_image* dst_img, const clk_image* src_img,
                           int32_t iterations, const clk_define* defines, size_t ndefines, void* stream) {
   t_error.clear();
+  TraceRange trace(kernel_name);
   const KernelInfo* k = find_kernel(kernel_name);
   if (!k) return fail(CLK_UNKNOWN_KERNEL, "unknown kernel '%s'", kernel_name ? kernel_name : "(null)");
   if (k->fam != F_MORPH) return fail(CLK_BAD_ARG, "%s is not a morphology kernel", k->name);
@@ -619,7 +631,7 @@ clk_status clk_morphology(const char* kernel_name, const clk_image* dst_img, con
   void* tmp = nullptr;
   if (nsteps > 1) {
     const size_t bytes = (size_t)dst.count() * dtype_size(dst.dt);
-    if (cudaMallocAsync(&tmp, bytes, stm) != cudaSuccess) {
+    if (alloc_failure_injected() || cudaMallocAsync(&tmp, bytes, stm) != cudaSuccess) {
       cudaGetLastError();
       return fail(CLK_OOM, "%s: cannot allocate a %zu-byte temporary", k->name, bytes);
     }

@@ -649,7 +649,7 @@ clk_status clk_batch_create(const clk_op* ops, int32_t nops, const clk_image* sr
     destroy(b);
     return CLK_NO_DEVICE;
   }
-  if (scratch && cudaMalloc(&b->scratch, scratch) != cudaSuccess) {
+  if (scratch && (alloc_failure_injected() || cudaMalloc(&b->scratch, scratch) != cudaSuccess)) {
     cudaGetLastError();
     destroy(b);
     return fail(CLK_OOM, "clk_batch_create: cannot allocate %zu bytes of intermediates", scratch);
@@ -783,6 +783,7 @@ clk_status clk_batch_create(const clk_op* ops, int32_t nops, const clk_image* sr
 }
 
 clk_status clk_batch_run(clk_batch* b, void* stream) {
+  TraceRange trace("clk_batch_run");
   if (!b || !b->exec) return fail(CLK_BAD_ARG, "clk_batch_run: no batch");
   if (cudaGraphLaunch(b->exec, (cudaStream_t)stream) != cudaSuccess) return check_launch("batch graph launch");
   count_launch(b->launches);

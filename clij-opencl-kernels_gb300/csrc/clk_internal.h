@@ -63,6 +63,21 @@ struct MedianNbhd {
 // error reporting (thread-local message) and launch accounting
 clk_status fail(clk_status st, const char* fmt, ...);
 void clear_error();  // empty the calling thread's message (start of every entry point)
+
+// Test hook for the out-of-memory branches: while the environment variable
+// CLK_INJECT_ALLOC_FAILURE is "1", every device allocation the library
+// makes for temporaries reports failure (as cudaMallocAsync would when the
+// device is full) and the caller sees CLK_OOM.
+bool alloc_failure_injected();
+
+// NVTX range around an entry point or a batch / server step (a named range
+// on the profiler's timeline; a no-op unless a tool is attached).
+struct TraceRange {
+  explicit TraceRange(const char* name);
+  ~TraceRange();
+  TraceRange(const TraceRange&) = delete;
+  TraceRange& operator=(const TraceRange&) = delete;
+};
 clk_status check_launch(const char* what);
 void count_launch(int n = 1);
 void uncount_launches(uint64_t n);  // launches recorded while capturing a graph

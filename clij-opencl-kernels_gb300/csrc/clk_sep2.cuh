@@ -46,6 +46,9 @@ struct Params {
   float hx[17], hy[17], hz[2 * kMaxCz + 1];
   float hs[3];
   int rte;
+  // TMA staging: polls of the wait for each staged tile before the CTA
+  // gives the tile up (tma::kWaitLimit unless CLK_TMA_WAIT_POLLS is set)
+  uint32_t tma_polls;
 };
 
 // ---------------------------------------------------------------- lanes

@@ -800,11 +800,17 @@ __device__ __forceinline__ void sep2_tile(const S* __restrict__ src, D* __restri
       if constexpr (TMA) {
         const int buf = it & 1;
         tcur = reinterpret_cast<S*>(reinterpret_cast<unsigned char*>(tin) + buf * G::buf_bytes());
-        if (tid == 0) stalled = tma::mbar_wait(&bars[buf], (it >> 1) & 1) ? 0 : 1;
+        if (tid == 0) stalled = tma::mbar_wait(&bars[buf], (it >> 1) & 1, p.tma_polls) ? 0 : 1;
         __syncthreads();  // tile landed; previous Y pass done with xs
-        if (stalled) {    // the copy never arrived: report, drain the other buffer, give up on this tile
+        if (stalled) {    // the copy did not arrive in time: report and give up on this tile
           if (tid == 0) {
             if (err) atomicExch(err, 1);
+            // every copy issued into this CTA's shared memory lands before
+            // the CTA exits: the abandoned one and the next plane's, each
+            // waited for with the full bound (a copy still missing after
+            // that is lost to the hardware; the flag already reports the
+            // launch as failed)
+            tma::mbar_wait(&bars[buf], (it >> 1) & 1);
             if (zi + 1 < z1 + cz) tma::mbar_wait(&bars[buf ^ 1], ((it + 1) >> 1) & 1);
           }
           return;
@@ -879,8 +885,20 @@ inline bool tma_enabled() {
   return on;
 }
 
+// CLK_TMA_WAIT_POLLS in the environment (read at every TMA launch): the
+// poll limit of the first wait for each staged tile; a test sets it to 0 to
+// make those waits run out.  Default tma::kWaitLimit.
+inline uint32_t tma_wait_polls() {
+  const char* e = getenv("CLK_TMA_WAIT_POLLS");
+  if (!e || !*e) return tma::kWaitLimit;
+  char* end = nullptr;
+  const unsigned long v = strtoul(e, &end, 10);
+  return (*end || v > tma::kWaitLimit) ? tma::kWaitLimit : (uint32_t)v;
+}
+
 template <class S, class D, int OP, int R>
-clk_status launch(const Image& dst, const Image& src, const Params& p, cudaStream_t st) {
+clk_status launch(const Image& dst, const Image& src, const Params& p_in, cudaStream_t st) {
+  Params p = p_in;
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -895,6 +913,7 @@ clk_status launch(const Image& dst, const Image& src, const Params& p, cudaStrea
   int* err = wait_flag_device();
   if (tma_enabled() && err && smem_ok(k_sep2_tma<S, D, OP, R>, GT::smem(p.cz)) &&
       tma::make_map_3d(&map, src.ptr, sizeof(S), src.w, src.h, src.d, GT::RW, GT::RH)) {
+    p.tma_polls = tma_wait_polls();
     k_sep2_tma<S, D, OP, R><<<grid, NT, GT::smem(p.cz), st>>>(map, (D*)dst.ptr, dst.w, dst.h, dst.d, zchunk, p, err);
     count_launch();
     return check_launch("separable (fused, sep2, tma)");

@@ -43,7 +43,7 @@ struct Request {
   double voxels = 0;
   Clock::time_point t_submit;
   std::atomic<int64_t> t_done_ns{0};  // stamped by the host callback
-  int state = 0;                      // 0 queued, 1 in flight, 2 done, 3 failed
+  int state = 0;                      // 0 queued, 1 in flight, 2 done, 3 failed, 4 cancelled
   clk_status status = CLK_OK;
   int slot = -1;
   void* tmp = nullptr;
@@ -73,7 +73,7 @@ struct clk_server {
   cudaMemPool_t pool = nullptr;
   int device = 0;
   int64_t budget = 0, in_use = 0, peak = 0;
-  uint64_t next_id = 1, submitted = 0, completed = 0, failed = 0;
+  uint64_t next_id = 1, submitted = 0, completed = 0, failed = 0, cancelled = 0;
   std::vector<double> latencies;
   double voxel_steps = 0;
   clk::Clock::time_point t0;
@@ -114,13 +114,14 @@ clk_status run_step(const Request& r, int k, const clk_image& in, const clk_imag
 
 // Enqueue a request's pipeline on its slot's stream (scheduler thread).
 void launch(clk_server* s, Request& r) {
+  TraceRange trace("clk_server request");
   cudaStream_t st = s->streams[r.slot];
   clk_status res = CLK_OK;
   const size_t in_bytes = image_bytes(r.src), out_bytes = image_bytes(r.dst);
   if (r.host_in && cudaMemcpyAsync(r.src.ptr, r.host_in, in_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
     res = check_launch("server: host->device copy");
   if (res == CLK_OK && r.tmp_bytes) {
-    if (cudaMallocFromPoolAsync(&r.tmp, r.tmp_bytes, s->pool, st) != cudaSuccess) {
+    if (alloc_failure_injected() || cudaMallocFromPoolAsync(&r.tmp, r.tmp_bytes, s->pool, st) != cudaSuccess) {
       cudaGetLastError();
       r.tmp = nullptr;
       res = fail(CLK_OOM, "server: request %llu: no memory for temporaries", (unsigned long long)r.id);
@@ -295,6 +296,29 @@ clk_status clk_server_wait(clk_server* s, uint64_t ticket, int32_t timeout_ms, d
   return r->status;
 }
 
+clk_status clk_server_cancel(clk_server* s, uint64_t ticket) {
+  if (!s) return fail(CLK_BAD_ARG, "clk_server_cancel: no server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->live.find(ticket);
+  if (it == s->live.end())
+    return fail(CLK_BAD_ARG, "clk_server_cancel: unknown ticket %llu", (unsigned long long)ticket);
+  auto r = it->second;
+  if (r->state != 0)
+    return fail(CLK_BUSY, "clk_server_cancel: request %llu is %s", (unsigned long long)ticket,
+                r->state == 1 ? "already running on the device" : "already finished");
+  for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
+    if (q->get() == r.get()) {
+      s->queue.erase(q);
+      break;
+    }
+  r->state = 4;
+  r->status = fail(CLK_CANCELLED, "request %llu was cancelled before it started", (unsigned long long)ticket);
+  s->cancelled++;
+  s->cv_done.notify_all();
+  s->cv_sched.notify_one();
+  return CLK_OK;
+}
+
 clk_status clk_server_drain(clk_server* s, int32_t timeout_ms) {
   if (!s) return fail(CLK_BAD_ARG, "clk_server_drain: no server");
   std::unique_lock<std::mutex> lk(s->mu);
@@ -312,6 +336,7 @@ clk_status clk_server_get_stats(clk_server* s, clk_server_stats* out) {
   st.submitted = s->submitted;
   st.completed = s->completed;
   st.failed = s->failed;
+  st.cancelled = s->cancelled;
   st.bytes_in_use = s->in_use;
   st.bytes_peak = s->peak;
   st.inflight = (int32_t)s->inflight.size();

@@ -5,7 +5,7 @@
 // signals an mbarrier with the byte count.  Out-of-range coordinates are
 // filled with zeros by the hardware; the kernels that use these loads replace
 // those with the clamp-to-edge values themselves.  Waits are bounded: after
-// kWaitLimit polls the waiter gives up and reports it, so a lost transfer can
+// a limit of polls the waiter gives up and reports it, so a lost transfer can
 // never hang the device.
 #pragma once
 #include <cuda.h>
@@ -73,11 +73,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
-// Poll the barrier's phase `parity` at most kWaitLimit times; true once it
-// completed, false if the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Poll the barrier's phase `parity` at most `limit` times; true once it
+// completed, false if the limit ran out (limit 0: false at once).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
   const uint32_t a = smem_addr(bar);
-  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+  for (uint32_t i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

@@ -41,7 +41,8 @@ typedef enum clk_status {
   CLK_LAUNCH_FAILED = 5,     /* CUDA reported an error                     */
   CLK_TIMEOUT = 6,           /* a bounded device wait ran out              */
   CLK_NO_DEVICE = 7,         /* no usable CUDA device                      */
-  CLK_BUSY = 8               /* admission refused (budget / slots)         */
+  CLK_BUSY = 8,              /* admission refused (budget / slots)         */
+  CLK_CANCELLED = 9          /* a served request was cancelled             */
 } clk_status;
 
 /* Pixel types of README.md:64-72 (char, uchar, short, ushort, float). */
@@ -269,6 +270,7 @@ typedef struct clk_server_stats {
   double p50_ms, p99_ms, mean_ms;    /* over completed requests */
   double voxel_steps;                /* sum over completed of voxels x steps */
   double busy_s;                     /* first submit -> last completion */
+  uint64_t cancelled;                /* requests cancelled before they ran */
 } clk_server_stats;
 
 /* slots: concurrent requests (streams), 1..64; hbm_budget_bytes: limit on
@@ -283,6 +285,11 @@ clk_status clk_server_submit(clk_server* server, const clk_op* ops, int32_t nops
 /* Wait (at most timeout_ms) for a request; CLK_TIMEOUT if it has not
  * finished; its latency in ms. */
 clk_status clk_server_wait(clk_server* server, uint64_t ticket, int32_t timeout_ms, double* latency_ms);
+/* Cancel a request that is still queued: it never runs, and waiting for
+ * its ticket returns CLK_CANCELLED.  A request already running on the
+ * device cannot be stopped (CLK_BUSY; wait for it instead); CLK_BAD_ARG for
+ * an unknown or already waited-for ticket. */
+clk_status clk_server_cancel(clk_server* server, uint64_t ticket);
 /* Wait (at most timeout_ms) until nothing is queued or in flight. */
 clk_status clk_server_drain(clk_server* server, int32_t timeout_ms);
 clk_status clk_server_get_stats(clk_server* server, clk_server_stats* out);
