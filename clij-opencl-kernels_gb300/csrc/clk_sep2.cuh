@@ -164,4 +164,12 @@ clk_status sep2_gauss(int R, const Image& dst, const Image& src, const float* wx
 clk_status sep2_gauss_exact(int R, const Image& dst, const Image& src, const float* const h[3], const float hs[3],
                             int cz, bool rte, cudaStream_t st);
 
+// The register-ring kernels of clk_sep3.cuh (16-bit pixels, x extent a
+// multiple of 8, small Z radius); CLK_UNSUPPORTED_DTYPE where they do not
+// apply, and the caller takes the kernels above.
+clk_status sep3_minmax(bool is_max, int R, const Image& dst, const Image& src, int cz, cudaStream_t st);
+clk_status sep3_mean(int R, const Image& dst, const Image& src, int cz, cudaStream_t st);
+clk_status sep3_gauss(int R, const Image& dst, const Image& src, const float* wx, const float* wy, const float* wz,
+                      int cz, cudaStream_t st);
+
 }  // namespace clk

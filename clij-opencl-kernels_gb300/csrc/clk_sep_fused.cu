@@ -26,6 +26,16 @@ namespace {
 
 using namespace fused;
 
+// CLK_SEP3=0 in the environment keeps the register-ring kernels out (A/B
+// timing against the shared-memory-ring kernels)
+bool sep3_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("CLK_SEP3");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 template <class S, class D, int OP, bool FAST, int KMAX>
 clk_status launch_fused(const Image& dst, const Image& src, const FusedTaps& ft, bool rte, cudaStream_t st) {
   const size_t smem = fused_smem(ft.c[0], ft.c[1], ft.c[2], sizeof(S), sizeof(D));
@@ -113,9 +123,11 @@ clk_status fused_separable(SepOp op, const Image& dst, const Image& src, const S
     const bool ints = src.dt == dst.dt && src.dt != CLK_F32;
     clk_status s2 = CLK_UNSUPPORTED_DTYPE;
     if ((op == SEP_MIN || op == SEP_MAX) && (ints || (src.dt == CLK_F32 && dst.dt == CLK_F32))) {
-      s2 = sep2_minmax(op == SEP_MAX, R, dst, src, cz, st);
+      if (sep3_enabled()) s2 = sep3_minmax(op == SEP_MAX, R, dst, src, cz, st);
+      if (s2 == CLK_UNSUPPORTED_DTYPE) s2 = sep2_minmax(op == SEP_MAX, R, dst, src, cz, st);
     } else if (op == SEP_MEAN && ints) {
-      s2 = sep2_mean(R, dst, src, cz, st);
+      if (sep3_enabled()) s2 = sep3_mean(R, dst, src, cz, st);
+      if (s2 == CLK_UNSUPPORTED_DTYPE) s2 = sep2_mean(R, dst, src, cz, st);
     } else if (op == SEP_GAUSS && ints) {
       // integer outputs: the reference's order and rounding, pass by pass
       const float* h[3] = {ft.h[0], ft.h[1], ft.h[2]};
@@ -129,7 +141,8 @@ clk_status fused_separable(SepOp op, const Image& dst, const Image& src, const S
         for (int v = 0; v <= 2 * c; ++v) sum += ft.h[d][v];
         for (int k = 0; k <= c; ++k) w[d][k] = (float)(ft.h[d][c + k] / sum);
       }
-      s2 = sep2_gauss(R, dst, src, w[0], w[1], w[2], cz, st);
+      if (sep3_enabled()) s2 = sep3_gauss(R, dst, src, w[0], w[1], w[2], cz, st);
+      if (s2 == CLK_UNSUPPORTED_DTYPE) s2 = sep2_gauss(R, dst, src, w[0], w[1], w[2], cz, st);
     }
     if (s2 != CLK_UNSUPPORTED_DTYPE) return s2;
   }
