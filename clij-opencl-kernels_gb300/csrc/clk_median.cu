@@ -17,10 +17,14 @@
 //    outputs of the planes above and below reuse;
 //  * box: the merge of planes z and z+1 (ranks 4..13) serves the outputs at
 //    z and z+1; each then needs one rank-9 selection against the third plane;
+//    8/16-bit pixels also pair rows y and y+1, whose blocks share two sorted
+//    rows (k_median_box27_yp);
 //  * sphere (8/16-bit): likewise the merge of planes z and z+1 (16 ranks)
 //    serves z and z+1, each adding its other plane's block and six singles;
 //  * the next z-pair's planes are loaded before the current pair's networks.
 // Borders clamp exactly as the reference's reads do.
+#include <cstdlib>
+
 #include "clk_median_impl.cuh"
 
 namespace clk {
@@ -40,6 +44,16 @@ Shape classify(bool sphere, const MedianNbhd& m, int ndim) {
   return OTHER;
 }
 
+// CLK_MEDIAN_YPAIR=0 in the environment keeps the box median on the
+// one-row kernel (A/B timing)
+bool ypair_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("CLK_MEDIAN_YPAIR");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 template <class T, bool ODD> clk_status launch(Shape sh, const Image& dst, const Image& src, cudaStream_t st) {
   const dim3 block(BX * BY);
   const int tx = ((src.w + 1) / 2 + BX - 1) / BX, ty = (src.h + BY - 1) / BY;
@@ -54,7 +68,17 @@ template <class T, bool ODD> clk_status launch(Shape sh, const Image& dst, const
     int zchunk = (src.d + chunks - 1) / chunks;
     zchunk += zchunk & 1;  // outputs come in z pairs
     const dim3 grid(tx, ty, (src.d + zchunk - 1) / zchunk);
-    if (sh == BOX27)
+    bool done = false;
+    if constexpr (sizeof(T) <= 2) {  // y pairs: 8/16-bit lanes (float keys would spill)
+      if (sh == BOX27 && ypair_enabled()) {
+        const dim3 gy(tx, (src.h + BYP - 1) / BYP, grid.z);
+        k_median_box27_yp<T, ODD><<<gy, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d,
+                                                        zchunk);
+        done = true;
+      }
+    }
+    if (done) {
+    } else if (sh == BOX27)
       k_median_box27<T, ODD><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);
     else if constexpr (sizeof(T) == 4)  // float keys: the pair kernel's registers would leave one CTA per SM
       k_median_sphere33<T, ODD><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);

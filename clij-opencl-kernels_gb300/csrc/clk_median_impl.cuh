@@ -224,6 +224,92 @@ __device__ __forceinline__ void box27_tile(const T* __restrict__ src, T* __restr
   }
 }
 
+// median_box_3d 3x3x3 for 8/16-bit pixels with y pairs: a thread computes
+// rows y and y+1 (and, as above, two x lanes and z pairs).  Their blocks
+// share rows y and y+1: per plane the four rows y-1 .. y+2 are sorted along
+// x once (net_sort3 of the lane words (x-1,x), (x,x+1), (x+1,x+2)), the two
+// shared rows merged once (net_merge33) and each block completed with its
+// own third row (net_merge63): 84 min/max for two sorted blocks instead of
+// 108.
+template <class T, bool ODD, class V>
+__device__ __forceinline__ void load_rows4(const T* plane, int x, int y, int W, int H, V (&q)[12]) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    row_cols<T, ODD>(plane + (int64_t)clampi(y - 1 + r, H - 1) * W, x, W, q[3 * r], q[3 * r + 1], q[3 * r + 2]);
+}
+template <class V> __device__ __forceinline__ void blocks_ypair(V (&q)[12], V (&b0)[9], V (&b1)[9]) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {  // each row's x-triple sorted in place
+    V t[3] = {q[3 * r], q[3 * r + 1], q[3 * r + 2]};
+    net_sort3_raw(t);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) q[3 * r + k] = t[net_sort3_out[k]];
+  }
+  V m[6];
+  {
+    V w[6] = {q[3], q[4], q[5], q[6], q[7], q[8]};  // rows y, y+1
+    net_merge33_raw(w);
+    pick(w, net_merge33_out, m);
+  }
+  {
+    V w[9] = {m[0], m[1], m[2], m[3], m[4], m[5], q[0], q[1], q[2]};  // + row y-1
+    net_merge63_raw(w);
+    pick(w, net_merge63_out, b0);
+  }
+  {
+    V w[9] = {m[0], m[1], m[2], m[3], m[4], m[5], q[9], q[10], q[11]};  // + row y+2
+    net_merge63_raw(w);
+    pick(w, net_merge63_out, b1);
+  }
+}
+
+constexpr int BYP = 2 * BY;  // rows per tile of the y-pair kernel
+
+template <class T, bool ODD>
+__device__ __forceinline__ void box27_ypair_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int D,
+                                                 int zchunk, int bx, int by, int bz) {
+  using V = typename Px<T>::V;
+  const int x = 2 * (bx * BX + (int)threadIdx.x % BX);
+  const int y = by * BYP + 2 * ((int)threadIdx.x / BX);
+  if (x >= W || y >= H) return;
+  const bool two = y + 1 < H;
+  const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+  auto pl = [&](int z) { return src + (int64_t)clampi(z, D - 1) * plane; };
+  V am1[9], bm1[9], a0[9], b0[9];  // sorted blocks (row y: a, row y+1: b) of planes zo-1, zo
+  V q1[12], q2[12];                // unsorted rows of planes zo+1, zo+2 (loaded one pair ahead)
+  load_rows4<T, ODD>(pl(z0 - 1), x, y, W, H, q1);
+  blocks_ypair(q1, am1, bm1);
+  load_rows4<T, ODD>(pl(z0), x, y, W, H, q1);
+  blocks_ypair(q1, a0, b0);
+  load_rows4<T, ODD>(pl(z0 + 1), x, y, W, H, q1);
+  load_rows4<T, ODD>(pl(z0 + 2), x, y, W, H, q2);
+  for (int zo = z0; zo < z1; zo += 2) {
+    V a1[9], b1[9], a2[9], b2[9];
+    blocks_ypair(q1, a1, b1);
+    blocks_ypair(q2, a2, b2);
+    if (zo + 2 < z1) {
+      load_rows4<T, ODD>(pl(zo + 3), x, y, W, H, q1);
+      load_rows4<T, ODD>(pl(zo + 4), x, y, W, H, q2);
+    }
+    T* o0 = dst + (int64_t)zo * plane + (int64_t)y * W;
+    {
+      V m[10];
+      merge_mid(a0, a1, m);
+      store_pair<T, ODD>(o0, x, W, final27(m, am1));
+      if (zo + 1 < z1) store_pair<T, ODD>(o0 + plane, x, W, final27(m, a2));
+    }
+    if (two) {
+      V m[10];
+      merge_mid(b0, b1, m);
+      store_pair<T, ODD>(o0 + W, x, W, final27(m, bm1));
+      if (zo + 1 < z1) store_pair<T, ODD>(o0 + plane + W, x, W, final27(m, b2));
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) am1[k] = a1[k], bm1[k] = b1[k], a0[k] = a2[k], b0[k] = b2[k];
+  }
+}
+
 // median_sphere_3d with Nx = Ny = Nz = 5: per output the 3x3 blocks of
 // planes z-1, z, z+1, the four voxels at distance 2 in plane z and the two
 // at distance 2 along z (33 = 9 + 9 + 9 + 4 + 2).
@@ -370,6 +456,11 @@ template <class T, bool ODD>
 __global__ void __launch_bounds__(BX * BY) k_median_box27(const T* __restrict__ src, T* __restrict__ dst, int W,
                                                           int H, int D, int zchunk) {
   box27_tile<T, ODD>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+template <class T, bool ODD>
+__global__ void __launch_bounds__(BX * BY, 2) k_median_box27_yp(const T* __restrict__ src, T* __restrict__ dst,
+                                                                 int W, int H, int D, int zchunk) {
+  box27_ypair_tile<T, ODD>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 // 16-bit pixels fit the sphere network in 64 registers without spilling:
 // four CTAs per SM instead of three

@@ -43,6 +43,36 @@ template <class V> CLK_NET_FN void net_merge333_raw(V (&w)[9]) {
 }
 CLK_NET_CONST int net_merge333_out[9] = {0, 1, 2, 4, 3, 5, 8, 7, 6};
 
+// sorted triples w[0..2], w[3..5] -> sorted 6
+// 12 min/max operations
+template <class V> CLK_NET_FN void net_merge33_raw(V (&w)[6]) {
+  { const V t = vmin(w[0], w[3]); w[3] = vmax(w[0], w[3]); w[0] = t; }
+  { const V t = vmin(w[2], w[5]); w[5] = vmax(w[2], w[5]); w[2] = t; }
+  { const V t = vmin(w[2], w[3]); w[3] = vmax(w[2], w[3]); w[2] = t; }
+  { const V t = vmin(w[1], w[4]); w[4] = vmax(w[1], w[4]); w[1] = t; }
+  { const V t = vmin(w[1], w[2]); w[2] = vmax(w[1], w[2]); w[1] = t; }
+  { const V t = vmin(w[4], w[3]); w[3] = vmax(w[4], w[3]); w[4] = t; }
+}
+CLK_NET_CONST int net_merge33_out[6] = {0, 1, 2, 4, 3, 5};
+
+// sorted 6 w[0..5] and sorted triple w[6..8] -> sorted 9
+// 24 min/max operations
+template <class V> CLK_NET_FN void net_merge63_raw(V (&w)[9]) {
+  { const V t = vmin(w[0], w[6]); w[6] = vmax(w[0], w[6]); w[0] = t; }
+  { const V t = vmin(w[4], w[6]); w[6] = vmax(w[4], w[6]); w[4] = t; }
+  { const V t = vmin(w[2], w[8]); w[8] = vmax(w[2], w[8]); w[2] = t; }
+  { const V t = vmin(w[2], w[4]); w[4] = vmax(w[2], w[4]); w[2] = t; }
+  { const V t = vmin(w[8], w[6]); w[6] = vmax(w[8], w[6]); w[8] = t; }
+  { const V t = vmin(w[1], w[7]); w[7] = vmax(w[1], w[7]); w[1] = t; }
+  { const V t = vmin(w[5], w[7]); w[7] = vmax(w[5], w[7]); w[5] = t; }
+  { const V t = vmin(w[3], w[5]); w[5] = vmax(w[3], w[5]); w[3] = t; }
+  { const V t = vmin(w[1], w[2]); w[2] = vmax(w[1], w[2]); w[1] = t; }
+  { const V t = vmin(w[3], w[4]); w[4] = vmax(w[3], w[4]); w[3] = t; }
+  { const V t = vmin(w[5], w[8]); w[8] = vmax(w[5], w[8]); w[5] = t; }
+  { const V t = vmin(w[7], w[6]); w[6] = vmax(w[7], w[6]); w[7] = t; }
+}
+CLK_NET_CONST int net_merge63_out[9] = {0, 1, 2, 3, 4, 5, 8, 7, 6};
+
 // sorted 9s w[0..8], w[9..17] -> ranks 4..13
 // 48 min/max operations
 template <class V> CLK_NET_FN void net_merge99_mid_raw(V (&w)[18]) {

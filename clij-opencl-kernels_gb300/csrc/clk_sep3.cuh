@@ -4,27 +4,26 @@
 //
 // A CTA (256 threads) owns a 64 x 32 column of outputs and streams along z,
 // one barrier per plane.  In the phase of plane i it
-//   stages  plane i+1: the clamped (32+2R) x (64+2RA) halo tile (RA = R
-//           rounded up to whole 16-byte vectors) enters shared memory as ROW
-//           PAIRS -- word (p, x) holds rows 2p and 2p+1 of column x in its two
-//           lanes (u16 lanes for min/max, an f32x2 pair for the Gaussian) --
-//           so that the X pass needs no byte permutes; the mean keeps plain
-//           rows (its sums are 32-bit);
-//   X pass  plane i: a thread filters one row pair x 8 outputs, the window
-//           sliding in registers (van Herk / Gil-Werman split for min/max:
-//           2R + 14 packed operations for 16 outputs; running sums for the
-//           mean; 8 accumulators for the Gaussian); results go back to plain
-//           rows, even and odd rows in two regions so that a warp's 16-byte
-//           stores hit distinct banks;
+//   X pass  plane i: a thread filters MX outputs of a ROW PAIR -- rows 2p
+//           and 2p+1 packed into the two lanes of each word by one byte
+//           permute per column (u16 lanes for min/max; an f32x2 pair for
+//           the Gaussian, converted once per staged pixel) -- so that every
+//           operation serves two rows; the window slides in registers (van
+//           Herk / Gil-Werman split for min/max: 2R + 2M - 2 packed
+//           operations for M outputs of both rows; running int32 sums for
+//           the mean, one row per task; 8 accumulators for the Gaussian);
+//           results go back to plain rows, even and odd rows in two regions
+//           so that a warp's 16-byte stores hit distinct banks;
 //   Y pass  plane i-1: a thread filters a column pair (x, x+1) x 4 rows;
 //   Z pass  the Y results enter a ring of the last 2CZ+1 planes held in the
 //           thread's REGISTERS (one copy of the ring step per slot, chosen
 //           by the slot counter, so that every slot is a fixed register);
 //           the thread reduces its ring and writes two pixels per store.
-// Staging: min / max / mean prefetch the next plane into registers during
-// the passes; the Gaussian, whose ring takes 88 registers, copies raw tiles
-// with cp.async (no registers) one plane ahead and converts them to f32x2
-// pairs in the next phase.
+// Staging: cp.async copies of the raw halo tile (no registers, no
+// instructions beyond one per 16-byte vector), rows clamped at the source;
+// min / max / mean copy two planes ahead into three buffers and the tiles
+// at the x border fill their outside vectors in shared memory; the Gaussian
+// converts each landed tile to f32x2 row pairs one phase ahead.
 //
 // Arithmetic (the same as the generic fused kernels, so the results are too):
 // min/max exact; the mean sums exactly in int32 and divides by a 32-bit
@@ -94,20 +93,20 @@ template <int OP, int R, int CZ, class C> struct Geo {
   static constexpr int NP = NR / 2;            // row pairs
   static constexpr int XOFF = RA - R;          // first staged column of the X windows
   static constexpr int NZ = 2 * CZ + 1;
-  static constexpr bool PAIRS = OP != MEAN;
-  // staging tasks: (vector, row pair) for the row-pair layouts, (vector, row) for the mean
-  static constexpr int NST = PAIRS ? NP * NV : NR * NV;
+  static constexpr bool PAIRS = OP != MEAN;    // X pass on row pairs
+  // staging: raw tiles (cp.async destinations), NRAW buffers of NR rows x SW
+  // pixels, pitch RWP.  Tasks: the Gaussian (vector, row pair), two copies
+  // each; the others (vector, row), one copy each.
+  static constexpr int NRAW = OP == GAUSS ? 2 : 3;
+  static constexpr int RWP = OP == GAUSS ? SW + 8 : SW;
+  static constexpr int RAW_BYTES = rup(NR * RWP * 2, 128);
+  static constexpr int NST = OP == GAUSS ? NP * NV : NR * NV;
   static constexpr int PST = (NST + NT - 1) / NT;
-  // staged tile: MIN/MAX u32 row-pair words, GAUSS f32x2 row pairs, MEAN u16
-  // rows; the pitch CW (entries) makes a warp's 16-byte X-pass reads, one row
-  // (pair) per thread, fall in distinct banks
-  static constexpr int CROWS = PAIRS ? NP : NR;
-  static constexpr int CW = OP == GAUSS ? SW + 2 : OP == MEAN ? (NV % 2 ? SW : SW + 8) : SW + 4;
-  static constexpr int CEL = OP == GAUSS ? 8 : OP == MEAN ? 2 : 4;
-  static constexpr int CV_BYTES = rup(CROWS * CW * CEL, 128);
-  // Gaussian raw tiles (cp.async destinations): NR rows of SW u16, pitch RWP
-  static constexpr int RWP = SW + 8;
-  static constexpr int RAW_BYTES = OP == GAUSS ? rup(NR * RWP * 2, 128) : 0;
+  // the Gaussian's converted tile: f32x2 row pairs, pitch CW entries (an odd
+  // number of 16-byte units: a warp's X reads, one row pair per thread, fall
+  // in distinct banks)
+  static constexpr int CW = SW + 2;
+  static constexpr int CV_BYTES = OP == GAUSS ? rup(NP * CW * 8, 128) : 0;
   // X results: NR rows x TX of u16 (f32 for GAUSS), pitch XP; the row-pair
   // layouts store even rows and odd rows in two regions (XHALF apart)
   static constexpr int XEL = OP == GAUSS ? 4 : 2;
@@ -115,8 +114,9 @@ template <int OP, int R, int CZ, class C> struct Geo {
   static constexpr int XHALF = NP * XP;
   static constexpr int XS_BYTES = rup(NR * XP * XEL, 128);
   static constexpr int XTASKS = (PAIRS ? NP : NR) * (TX / MX);
-  static constexpr int SMEM = 2 * RAW_BYTES + 2 * CV_BYTES + 2 * XS_BYTES;
-  static constexpr int NWX = rup(XOFF + MX + 2 * R, OP == GAUSS ? 2 : OP == MEAN ? 8 : 4);  // entries read per X task
+  static constexpr int SMEM = NRAW * RAW_BYTES + 2 * CV_BYTES + 2 * XS_BYTES;
+  // pixels (Gaussian: f32x2 entries) an X task reads from the start of its segment
+  static constexpr int NWX = rup(XOFF + MX + 2 * R, OP == GAUSS ? 2 : 8);
 };
 
 template <bool SG, int OP> __device__ __forceinline__ uint32_t mm(uint32_t a, uint32_t b) {
@@ -125,32 +125,32 @@ template <bool SG, int OP> __device__ __forceinline__ uint32_t mm(uint32_t a, ui
 }
 
 // out[j] = op(win[j .. j+2R]) for j < M: the van Herk / Gil-Werman split
-// (2R + 2M - 2 operations) when every window contains column M, else direct
-template <bool SG, int OP, int M, int R>
+// (2R + 2M - 2 operations) when every window contains column M; longer runs
+// in pieces of 2R outputs; direct for a single output
+template <bool SG, int OP, int M, int R, int O = 0>
 __device__ __forceinline__ void slide_minmax(const uint32_t (&win)[M + 2 * R], uint32_t (&out)[M]) {
-  if constexpr (2 * R >= M && M > 1) {
-    uint32_t suf[M];
-    suf[M - 1] = win[M - 1];
+  constexpr int B = (2 * R < M - O) ? 2 * R : M - O;  // outputs O .. O+B-1 in this piece
+  if constexpr (B > 1) {
+    uint32_t suf[B];
+    suf[B - 1] = win[O + B - 1];
 #pragma unroll
-    for (int j = M - 2; j >= 0; --j) suf[j] = mm<SG, OP>(win[j], suf[j + 1]);
-    uint32_t pre = win[M];
+    for (int j = B - 2; j >= 0; --j) suf[j] = mm<SG, OP>(win[O + j], suf[j + 1]);
+    uint32_t pre = win[O + B];
 #pragma unroll
-    for (int k = M + 1; k <= 2 * R; ++k) pre = mm<SG, OP>(pre, win[k]);
-    out[0] = mm<SG, OP>(suf[0], pre);
+    for (int k = B + 1; k <= 2 * R; ++k) pre = mm<SG, OP>(pre, win[O + k]);
+    out[O] = mm<SG, OP>(suf[0], pre);
 #pragma unroll
-    for (int j = 1; j < M; ++j) {
-      pre = mm<SG, OP>(pre, win[j + 2 * R]);
-      out[j] = mm<SG, OP>(suf[j], pre);
+    for (int j = 1; j < B; ++j) {
+      pre = mm<SG, OP>(pre, win[O + j + 2 * R]);
+      out[O + j] = mm<SG, OP>(suf[j], pre);
     }
   } else {
+    uint32_t a = win[O];
 #pragma unroll
-    for (int j = 0; j < M; ++j) {
-      uint32_t a = win[j];
-#pragma unroll
-      for (int k = 1; k <= 2 * R; ++k) a = mm<SG, OP>(a, win[j + k]);
-      out[j] = a;
-    }
+    for (int k = 1; k <= 2 * R; ++k) a = mm<SG, OP>(a, win[O + k]);
+    out[O] = a;
   }
+  if constexpr (O + B < M) slide_minmax<SG, OP, M, R, O + B>(win, out);
 }
 
 template <bool SG> __device__ __forceinline__ int lane_lo(uint32_t w) {
@@ -167,6 +167,7 @@ __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // (row a, row b) of element e of two 8-pixel u16 vectors as an exact f32x2:
 // the float 2^23 + v built by a byte permute, minus 2^23 (unsigned pixels)
@@ -188,96 +189,80 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
   static_assert(G::XTASKS <= NT, "one X task per thread");
   extern __shared__ __align__(128) unsigned char smem[];
   // byte offsets of the buffers in shared memory
-  constexpr uint32_t RAW0 = 0, CV0 = 2 * G::RAW_BYTES, XS0 = CV0 + 2 * G::CV_BYTES;
+  constexpr uint32_t RAW0 = 0, CV0 = G::NRAW * G::RAW_BYTES, XS0 = CV0 + 2 * G::CV_BYTES;
 
   const int tid = threadIdx.x;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int z0 = blockIdx.z * zchunk, z1 = min(Dz, z0 + zchunk);
   const size_t plane = (size_t)W * H;
+  // a tile whose staged columns reach past the image: its outside vectors
+  // are filled in shared memory (rows are clamped at the source)
+  const bool xborder = x0 - G::RA < 0 || x0 + TX + G::RA > W;
 
-  // ---- staging tasks of this thread (the same for every plane): in-plane
-  // offsets of the rows' 16-byte vectors; a vector outside its row is the
-  // row's edge pixel repeated (bit k of splat).  Rows and the staged origin
-  // are vector-aligned (W % 8 == 0): a vector is wholly inside or outside.
-  uint32_t offa[G::PST], offb[G::PST], cst[G::PST];
-  uint32_t splat = 0, svalid = 0;
+  // ---- staging tasks of this thread (the same for every plane): the
+  // in-plane offset of each copied 16-byte vector (rows clamped) and its
+  // place in the raw tile; vectors outside their row are not copied (bit k
+  // of outside) but repeat the row's edge pixel.  Rows and the staged
+  // origin are vector-aligned (W % 8 == 0): a vector is wholly inside or
+  // outside.
+  uint32_t goff[G::PST], soff[G::PST], eoff[G::PST];
+  uint32_t valid = 0, outside = 0;
 #pragma unroll
   for (int k = 0; k < G::PST; ++k) {
     const int q = tid + k * NT;
-    offa[k] = offb[k] = cst[k] = 0;
+    goff[k] = soff[k] = eoff[k] = 0;
     if (q < G::NST) {
-      svalid |= 1u << k;
+      valid |= 1u << k;
       const int v = q % G::NV, r = q / G::NV;
       const int gx = x0 - G::RA + 8 * v;
-      const int cx = gx < 0 ? 0 : gx >= W ? W - 1 : gx;
-      if (cx != gx) splat |= 1u << k;
-      const int ra = G::PAIRS ? 2 * r : r;
-      offa[k] = (uint32_t)clampi(y0 - R + ra, H - 1) * (uint32_t)W + (uint32_t)cx;
-      offb[k] = (uint32_t)clampi(y0 - R + ra + 1, H - 1) * (uint32_t)W + (uint32_t)cx;
-      if constexpr (OP == GAUSS) cst[k] = (uint32_t)((2 * r) * G::RWP + 8 * v) * 2;  // raw row 2r, vector v
-      else cst[k] = (uint32_t)(r * G::CW + 8 * v) * G::CEL;
+      const int ra = OP == GAUSS ? 2 * r : r;  // first staged row of the task
+      if (gx < 0 || gx >= W) {
+        outside |= 1u << k;
+        eoff[k] = (uint32_t)(ra * G::RWP + (gx < 0 ? 0 : W - 1) - (x0 - G::RA)) * 2;  // the row's edge pixel
+      }
+      goff[k] = (uint32_t)clampi(y0 - R + ra, H - 1) * (uint32_t)W + (uint32_t)min(max(gx, 0), W - 8);
+      soff[k] = (uint32_t)(ra * G::RWP + 8 * v) * 2;
     }
   }
-
-  // ---- register prefetch (min / max / mean)
-  uint4 pa[G::PST], pb[G::PST];
-  auto fetch = [&](int zv) {
-    const S* sp = src + (size_t)clampi(zv, Dz - 1) * plane;
+  uint32_t goff2[OP == GAUSS ? G::PST : 1];  // the Gaussian's second row
 #pragma unroll
-    for (int k = 0; k < G::PST; ++k) {
-      if (svalid >> k & 1) {
-        if (splat >> k & 1) {
-          const uint32_t a = splat16((uint16_t)__ldg(sp + offa[k]));
-          pa[k] = make_uint4(a, a, a, a);
-          if constexpr (G::PAIRS) {
-            const uint32_t b = splat16((uint16_t)__ldg(sp + offb[k]));
-            pb[k] = make_uint4(b, b, b, b);
-          }
-        } else {
-          pa[k] = __ldg(reinterpret_cast<const uint4*>(sp + offa[k]));
-          if constexpr (G::PAIRS) pb[k] = __ldg(reinterpret_cast<const uint4*>(sp + offb[k]));
-        }
-      }
+  for (int k = 0; k < (OP == GAUSS ? G::PST : 1); ++k) {
+    goff2[k] = 0;
+    const int q = tid + k * NT;
+    if (OP == GAUSS && q < G::NST) {
+      const int v = q % G::NV, r = q / G::NV;
+      const int gx = x0 - G::RA + 8 * v;
+      goff2[k] = (uint32_t)clampi(y0 - R + 2 * r + 1, H - 1) * (uint32_t)W + (uint32_t)min(max(gx, 0), W - 8);
     }
-  };
-  auto commit = [&](uint32_t cvo) {  // cvo: byte offset of the staged-tile buffer
-#pragma unroll
-    for (int k = 0; k < G::PST; ++k) {
-      if (svalid >> k & 1) {
-        unsigned char* d = smem + cvo + cst[k];
-        if constexpr (G::PAIRS) {
-          const uint32_t a[4] = {pa[k].x, pa[k].y, pa[k].z, pa[k].w}, b[4] = {pb[k].x, pb[k].y, pb[k].z, pb[k].w};
-          uint32_t o[8];
-#pragma unroll
-          for (int m = 0; m < 4; ++m) o[2 * m] = __byte_perm(a[m], b[m], 0x5410), o[2 * m + 1] = __byte_perm(a[m], b[m], 0x7632);
-          reinterpret_cast<uint4*>(d)[0] = make_uint4(o[0], o[1], o[2], o[3]);
-          reinterpret_cast<uint4*>(d)[1] = make_uint4(o[4], o[5], o[6], o[7]);
-        } else {
-          *reinterpret_cast<uint4*>(d) = pa[k];
-        }
-      }
-    }
-  };
-
-  // ---- Gaussian staging: cp.async raw tiles, converted one phase later
+  }
   auto issue_raw = [&](int zv, uint32_t rwo) {
     const S* sp = src + (size_t)clampi(zv, Dz - 1) * plane;
 #pragma unroll
     for (int k = 0; k < G::PST; ++k) {
-      if ((svalid & ~splat) >> k & 1) {
-        cp_async16(smem + rwo + cst[k], sp + offa[k]);
-        cp_async16(smem + rwo + cst[k] + G::RWP * 2, sp + offb[k]);
+      if ((valid & ~outside) >> k & 1) {
+        cp_async16(smem + rwo + soff[k], sp + goff[k]);
+        if constexpr (OP == GAUSS) cp_async16(smem + rwo + soff[k] + G::RWP * 2, sp + goff2[k]);
       }
     }
     cp_async_commit();
   };
-  // convert tasks: (row pair yp, vector v), yp fastest; raw -> f32x2 pairs;
-  // a vector outside its row repeats the edge pixel, read from the raw tile
-  // where the row's first / last vector sits
-  uint32_t crd[G::PST], cwr[G::PST];
+  // min / max / mean: the outside vectors of a landed raw tile repeat their
+  // row's edge pixel (x-border tiles only)
+  auto fixup = [&](uint32_t rwo) {
+#pragma unroll
+    for (int k = 0; k < G::PST; ++k) {
+      if (outside >> k & 1) {
+        const uint32_t e = splat16(*reinterpret_cast<const uint16_t*>(smem + rwo + eoff[k]));
+        *reinterpret_cast<uint4*>(smem + rwo + soff[k]) = make_uint4(e, e, e, e);
+      }
+    }
+  };
+  // Gaussian: raw -> f32x2 row pairs, tasks (row pair yp, vector v), yp
+  // fastest; a vector outside its row repeats the edge pixel
+  uint32_t crd[OP == GAUSS ? G::PST : 1], cwr[OP == GAUSS ? G::PST : 1];
   uint32_t cedge = 0;
 #pragma unroll
-  for (int k = 0; k < G::PST; ++k) {
+  for (int k = 0; k < (OP == GAUSS ? G::PST : 1); ++k) {
     const int q = tid + k * NT;
     crd[k] = cwr[k] = 0;
     if (OP == GAUSS && q < G::NST) {
@@ -294,8 +279,8 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
   }
   auto convert = [&](uint32_t rwo, uint32_t cvo) {
 #pragma unroll
-    for (int k = 0; k < G::PST; ++k) {
-      if (svalid >> k & 1) {
+    for (int k = 0; k < (OP == GAUSS ? G::PST : 1); ++k) {
+      if (valid >> k & 1) {
         const unsigned char* s = smem + rwo + crd[k];
         uint4 a, b;
         if (cedge >> k & 1) {
@@ -315,38 +300,45 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
     }
   };
 
-  // ---- X task of this thread (at most one): row pair (row for the mean)
-  // xr, segment xs of MX outputs; byte offsets of its reads and writes
+  // ---- X task of this thread (at most one).  Min / max / mean: segment xsg
+  // of MX outputs fastest, then the row pair (row for the mean), so a warp's
+  // 16-byte reads and writes are contiguous; the Gaussian: row pair fastest
+  // (the converted tile's pitch spreads those over the banks).
   const bool xvalid = tid < G::XTASKS;
   uint32_t xrd = 0, xwr = 0;
   {
     const int q = xvalid ? tid : 0;
-    const int xr = q % G::CROWS, xsg = q / G::CROWS;
-    if constexpr (OP == MIN || OP == MAX) {
-      xrd = (uint32_t)(xr * G::CW + MX * xsg) * 4;
-      xwr = (uint32_t)(xr * G::XP + MX * xsg) * 2;  // even region row xr = tile row 2xr
-    } else if constexpr (OP == MEAN) {
-      xrd = (uint32_t)(xr * G::CW + MX * xsg) * 2;
-      xwr = (uint32_t)(xr * G::XP + MX * xsg) * 2;
+    if constexpr (OP == GAUSS) {
+      const int xr = q % G::NP, xsg = q / G::NP;
+      xrd = (uint32_t)(xr * G::CW + 8 * xsg + (G::XOFF & ~1)) * 8;
+      xwr = (uint32_t)(xr * G::XP + 8 * xsg) * 4;
     } else {
-      xrd = (uint32_t)(xr * G::CW + MX * xsg + (G::XOFF & ~1)) * 8;
-      xwr = (uint32_t)(xr * G::XP + MX * xsg) * 4;
+      constexpr int NSG = TX / MX;
+      const int xsg = q % NSG, xr = q / NSG;
+      xrd = (uint32_t)((G::PAIRS ? 2 * xr : xr) * G::RWP + MX * xsg) * 2;
+      xwr = (uint32_t)(xr * G::XP + MX * xsg) * 2;  // row-pair layouts: even region row xr = tile row 2xr
     }
   }
-  auto xpass = [&](uint32_t cvo, uint32_t xso) {
+  auto xpass = [&](uint32_t rwo, uint32_t cvo, uint32_t xso) {
     if (!xvalid) return;
-    const unsigned char* rowp = smem + cvo + xrd;
     unsigned char* xe = smem + xso + xwr;
     if constexpr (OP == MIN || OP == MAX) {
-      uint32_t w[G::NWX];
+      const unsigned char* ra = smem + rwo + xrd;
+      const unsigned char* rb = ra + G::RWP * 2;
+      uint32_t wa[G::NWX / 2], wb[G::NWX / 2];
 #pragma unroll
-      for (int m = 0; m < G::NWX / 4; ++m) {
-        const uint4 t = reinterpret_cast<const uint4*>(rowp)[m];
-        w[4 * m] = t.x, w[4 * m + 1] = t.y, w[4 * m + 2] = t.z, w[4 * m + 3] = t.w;
+      for (int m = 0; m < G::NWX / 8; ++m) {
+        const uint4 t = reinterpret_cast<const uint4*>(ra)[m], u = reinterpret_cast<const uint4*>(rb)[m];
+        wa[4 * m] = t.x, wa[4 * m + 1] = t.y, wa[4 * m + 2] = t.z, wa[4 * m + 3] = t.w;
+        wb[4 * m] = u.x, wb[4 * m + 1] = u.y, wb[4 * m + 2] = u.z, wb[4 * m + 3] = u.w;
       }
+      // row pairs (row 2yp low lane, row 2yp+1 high lane) of the window
       uint32_t win[MX + 2 * R], o[MX];
 #pragma unroll
-      for (int j = 0; j < MX + 2 * R; ++j) win[j] = w[G::XOFF + j];
+      for (int j = 0; j < MX + 2 * R; ++j) {
+        const int e = G::XOFF + j;
+        win[j] = __byte_perm(wa[e >> 1], wb[e >> 1], (e & 1) ? 0x7632 : 0x5410);
+      }
       slide_minmax<SG, OP, MX, R>(win, o);
       unsigned char* xo = xe + G::XHALF * 2;  // odd rows
 #pragma unroll
@@ -358,6 +350,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
                                                      __byte_perm(t[4], t[5], 0x7632), __byte_perm(t[6], t[7], 0x7632));
       }
     } else if constexpr (OP == MEAN) {
+      const unsigned char* rowp = smem + rwo + xrd;
       uint32_t w[G::NWX / 2];
 #pragma unroll
       for (int m = 0; m < G::NWX / 8; ++m) {
@@ -382,6 +375,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
                                                      __byte_perm(t[4], t[5], 0x5410), __byte_perm(t[6], t[7], 0x5410));
       }
     } else {  // GAUSS: 8 accumulators, each entry added to every output it reaches
+      const unsigned char* rowp = smem + cvo + xrd;
       constexpr int E0 = G::XOFF & ~1;  // first entry read (16-byte aligned)
       uint64_t acc[8];
 #pragma unroll
@@ -516,8 +510,11 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
     outp += plane;
   };
 
-  // ---- the plane loop: phase it stages plane it+1, X-filters plane it and
-  // Y/Z-filters plane it-1; one barrier per phase.
+  // ---- the plane loop: phase it X-filters plane it and Y/Z-filters plane
+  // it-1 while the copy of a later plane is in flight; one barrier per phase
+  // (x-border tiles: two, the second after filling the outside vectors).
+  // Min / max / mean: three raw buffers, plane it+2 copied during phase it.
+  // Gaussian: two raw buffers, plane it+1 converted during phase it.
   const int NPL = (z1 - z0) + 2 * CZ;  // planes z0-CZ .. z1+CZ-1
   if constexpr (OP == GAUSS) {
     issue_raw(z0 - CZ, RAW0);
@@ -527,26 +524,32 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
     convert(RAW0, CV0);
     __syncthreads();
   } else {
-    fetch(z0 - CZ);
-    commit(CV0);
-    if (NPL > 1) fetch(z0 - CZ + 1);
+    issue_raw(z0 - CZ, RAW0);
+    issue_raw(z0 - CZ + 1, RAW0 + G::RAW_BYTES);
+    cp_async_wait_1();
     __syncthreads();
+    if (xborder) {
+      fixup(RAW0);
+      __syncthreads();
+    }
   }
   int slot = 0;  // ring slot of the next Y plane
+  int rcur = 0;  // raw buffer of plane it (min / max / mean: it % 3)
   for (int it = 0; it <= NPL; ++it) {
     const uint32_t cur = it & 1, nxt = cur ^ 1;
-    if (it < NPL) {
+    if constexpr (OP == GAUSS) {
       if (it + 1 < NPL) {
-        if constexpr (OP == GAUSS) {
-          // raw(it), in buffer cur, was converted in phase it-1
-          if (it + 2 < NPL) issue_raw(z0 - CZ + it + 2, RAW0 + cur * G::RAW_BYTES);
-          convert(RAW0 + nxt * G::RAW_BYTES, CV0 + nxt * G::CV_BYTES);
-        } else {
-          commit(CV0 + nxt * G::CV_BYTES);
-          if (it + 2 < NPL) fetch(z0 - CZ + it + 2);
-        }
+        // raw(it), in buffer cur, was converted in phase it-1
+        if (it + 2 < NPL) issue_raw(z0 - CZ + it + 2, RAW0 + cur * G::RAW_BYTES);
+        convert(RAW0 + nxt * G::RAW_BYTES, CV0 + nxt * G::CV_BYTES);
       }
-      xpass(CV0 + cur * G::CV_BYTES, XS0 + cur * G::XS_BYTES);
+      if (it < NPL) xpass(0, CV0 + cur * G::CV_BYTES, XS0 + cur * G::XS_BYTES);
+    } else {
+      // buffer (it+2) % 3 held plane it-1, whose X pass ended in phase it-1
+      const int r2 = rcur == 0 ? 2 : rcur - 1;
+      if (it + 2 < NPL) issue_raw(z0 - CZ + it + 2, RAW0 + r2 * G::RAW_BYTES);
+      else cp_async_commit();  // an empty group keeps the group count per phase at one
+      if (it < NPL) xpass(RAW0 + rcur * G::RAW_BYTES, 0, XS0 + cur * G::XS_BYTES);
     }
     if (it >= 1) {
       if (yvalid) {
@@ -558,8 +561,19 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
       }
       slot = slot + 1 == NZ ? 0 : slot + 1;
     }
-    if constexpr (OP == GAUSS) cp_async_wait_all();
-    __syncthreads();
+    if constexpr (OP == GAUSS) {
+      cp_async_wait_all();
+      __syncthreads();
+    } else {
+      cp_async_wait_1();  // plane it+1 has landed (plane it+2 may still be in flight)
+      __syncthreads();
+      const int r1 = rcur == 2 ? 0 : rcur + 1;
+      if (xborder && it + 1 < NPL) {
+        fixup(RAW0 + r1 * G::RAW_BYTES);
+        __syncthreads();
+      }
+      rcur = r1;
+    }
   }
 }
 
@@ -597,7 +611,10 @@ inline int chunk_count(int tiles, int depth, int cz, int ctas_per_sm) {
 
 // the launch shape of each operation
 template <int OP, int CZ> struct DefaultCfg {
-  typedef Cfg<256, 4, 16, OP == GAUSS ? 2 : CZ >= 3 ? 3 : 4> type;
+  // measured on 1024 x 1024 x 256 u16 (r5, cz 2): min / max 0.290 ms with
+  // 8 outputs per X task (van Herk pieces of 8), 0.318 with 16; the mean
+  // needs 16 (one X task per thread)
+  typedef Cfg<256, 4, OP == MEAN ? 16 : 8, OP == GAUSS ? 2 : CZ >= 3 ? 3 : 4> type;
 };
 
 template <class S, int OP, int R, int CZ, class C = typename DefaultCfg<OP, CZ>::type>

@@ -27,11 +27,13 @@ namespace {
 using namespace fused;
 
 // CLK_SEP3=0 in the environment keeps the register-ring kernels out (A/B
-// timing against the shared-memory-ring kernels)
+// timing against the shared-memory-ring kernels); so does CLK_SEP2_TMA=1,
+// which asks for the shared-memory-ring kernels' TMA staging
 bool sep3_enabled() {
   static const bool on = [] {
     const char* e = getenv("CLK_SEP3");
-    return !(e && e[0] == '0');
+    const char* t = getenv("CLK_SEP2_TMA");
+    return !(e && e[0] == '0') && !(t && t[0] == '1');
   }();
   return on;
 }

@@ -16,8 +16,10 @@ principle: exhaustively over the ones-counts of its sorted groups and every
 0/1 pattern of its free wires) and on random values.
 
 Networks (V is a SIMD word: two 16-bit lanes, one output each):
-  net_sort3            sort three values (a z- or y-column)
+  net_sort3            sort three values (a z- or y-column, or an x-row)
   net_merge333         three sorted triples -> sorted 9 (3x3 block of a plane)
+  net_merge33          two sorted triples -> sorted 6 (rows shared by a y pair)
+  net_merge63          sorted 6 + sorted triple -> sorted 9
   net_merge99_mid      two sorted 9s -> ranks 4..13 of their merge
   net_box27_final      rank 9 of (ranks 4..13 of 18) U (sorted 9) = median of 27
   net_sphere33_final   rank 16 of (sorted 9 U sorted 9 U sorted 9 U 4 U 2) = median of 33
@@ -162,6 +164,24 @@ def main():
     verify(prog, 9, [[0, 1, 2], [3, 4, 5], [6, 7, 8]], lambda v, o: [o[w] for w in r] == sorted(v))
     stats["merge333"] = ops(prog)
     parts.append(("net_merge333_raw", 9, prog, r, "three sorted triples w[0..2], w[3..5], w[6..8] -> sorted 9"))
+
+    # merge33: two sorted triples w[0..2], w[3..5] -> sorted 6 (the two rows
+    # a y-pair of box-median outputs shares)
+    net = []
+    r = oe_merge([0, 1, 2], [3, 4, 5], net)
+    prog = prune(net, r)
+    verify(prog, 6, [[0, 1, 2], [3, 4, 5]], lambda v, o: [o[w] for w in r] == sorted(v))
+    stats["merge33"] = ops(prog)
+    parts.append(("net_merge33_raw", 6, prog, r, "sorted triples w[0..2], w[3..5] -> sorted 6"))
+
+    # merge63: sorted 6 w[0..5] and sorted triple w[6..8] -> sorted 9 (a
+    # 3x3 block from the shared pair of rows and its own third row)
+    net = []
+    r = oe_merge(list(range(6)), [6, 7, 8], net)
+    prog = prune(net, r)
+    verify(prog, 9, [list(range(6)), [6, 7, 8]], lambda v, o: [o[w] for w in r] == sorted(v))
+    stats["merge63"] = ops(prog)
+    parts.append(("net_merge63_raw", 9, prog, r, "sorted 6 w[0..5] and sorted triple w[6..8] -> sorted 9"))
 
     # merge99_mid: wires 0-8 and 9-17 sorted -> ranks 4..13
     net = []

@@ -105,3 +105,39 @@ def test_server_errors(clk):
     with pytest.raises(clk.ClkError):
         srv.wait(123456789)
     srv.close()
+
+
+def oracle_pipeline(clk, oracle, ops, a):
+    """The request's steps on the CPU, one oracle call per reference launch:
+    separable filters X -> Y (-> Z) with dst-typed temporaries, median and
+    sobel as one launch each, radius-r morphology as r launches of the r=1
+    kernel; every intermediate in the request's pixel type."""
+    from clk import _lib as L
+    nd = a.ndim
+    sfx = "_2d" if nd == 2 else "_3d"
+    cur = a
+    for op in ops:
+        name = op["kernel"] + sfx
+        if op["kind"] == L.OP_SEPARABLE:
+            cur = oracle.separable(name, cur, a.dtype, op["N"][:nd], op["s"][:nd])
+        elif op["kind"] == L.OP_MORPHOLOGY:
+            for _ in range(op["iterations"]):
+                cur = oracle.execute(name, cur, a.dtype)
+        elif op["kernel"].startswith("median"):
+            cur = oracle.execute(name, cur, a.dtype, op["N"][:nd])
+        else:
+            cur = oracle.execute(name, cur, a.dtype)
+    return cur
+
+
+def test_served_integer_results_match_the_oracle(clk, oracle):
+    # Integer requests served in the mix (8 slots, all in flight) against the
+    # oracle run step by step: bit for bit.
+    import torch
+    rng = np.random.default_rng(63)
+    reqs = [r for r in make_requests(clk, rng, 60) if r[1].dtype != torch.float32]
+    mixed, st = serve(clk, reqs, slots=8)
+    assert st["completed"] == len(reqs) and st["failed"] == 0
+    for k, ((ops, src), got) in enumerate(zip(reqs, mixed)):
+        want = oracle_pipeline(clk, oracle, ops, src.cpu().numpy())
+        assert np.array_equal(got, want), (k, src.shape, src.dtype, [o["kernel"] for o in ops])
