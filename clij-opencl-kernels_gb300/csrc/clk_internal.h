@@ -176,6 +176,10 @@ clk_status fused_separable(SepOp op, const Image& dst, const Image& src, const S
 clk_status fast_morph(bool erode, bool sphere, int iterations, const Image& dst, const Image& src, const Policy& p,
                       cudaStream_t st, bool planar = false);
 bool fast_morph_fusable(const Image& dst, const Image& src);  // fast_morph takes iterations = 2
+// the bit-word kernels (clk_morph_bits.cu): 8-bit 3-D images with rows of
+// whole 32-voxel words, one or two iterations; CLK_UNSUPPORTED_DTYPE where
+// they do not apply
+clk_status morph_bits(bool erode, bool sphere, int iterations, const Image& dst, const Image& src, cudaStream_t st);
 clk_status fast_sobel(const Image& dst, const Image& src, const Policy& p, cudaStream_t st);
 clk_status fast_median(bool sphere, const Image& dst, const Image& src, const MedianNbhd& m, cudaStream_t st);
 

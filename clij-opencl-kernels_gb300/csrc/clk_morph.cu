@@ -16,6 +16,8 @@
 // the value at the clamped position -- not the operator re-evaluated on
 // clamped inputs.  The fused kernel therefore copies border rows and planes
 // of the intermediate instead of computing them.
+#include <cstdlib>
+
 #include "clk_common.cuh"
 
 namespace clk {
@@ -264,6 +266,15 @@ clk_status launch_sel(const Image& dst, const Image& src, cudaStream_t st) {
   return launch_morph<int8_t, int8_t, ERODE, SPHERE, ITER>(dst, src, st);
 }
 
+// CLK_MORPH_BITS=0 in the environment keeps the byte-mask kernels (A/B timing)
+bool morph_bits_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("CLK_MORPH_BITS");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 }  // namespace
 
 bool fast_morph_fusable(const Image& dst, const Image& src) {
@@ -275,6 +286,10 @@ bool fast_morph_fusable(const Image& dst, const Image& src) {
 clk_status fast_morph(bool erode, bool sphere, int iterations, const Image& dst, const Image& src, const Policy&,
                       cudaStream_t st, bool planar) {
   if (!fast_morph_fusable(dst, src) || iterations < 1 || iterations > 2) return CLK_UNSUPPORTED_DTYPE;
+  if (!planar && morph_bits_enabled()) {
+    const clk_status b = morph_bits(erode, sphere, iterations, dst, src, st);
+    if (b != CLK_UNSUPPORTED_DTYPE) return b;
+  }
   if (planar) {
     if (iterations != 1) return CLK_UNSUPPORTED_DTYPE;
     if (erode) return sphere ? launch_sel<true, true, 0>(dst, src, st) : launch_sel<true, false, 0>(dst, src, st);

@@ -79,3 +79,21 @@ def test_2d_morphology(clk, oracle):
         a = random_image(rng, (45, 64), np.uint8, binary=True, density=0.7)
         for it in (1, 2):
             assert np.array_equal(run(clk, kernel, a, np.uint8, it), oracle_iter(oracle, kernel, a, np.uint8, it))
+
+
+@pytest.mark.parametrize("kernel", MORPH[:4])
+def test_bit_words_any_nonzero_byte(clk, oracle, kernel):
+    # Rows of whole 32-voxel words take the bit-word kernels: every nonzero
+    # byte value counts as set (signed and unsigned pixels), borders clamp,
+    # one and two iterations per pass (and chains of them), results bit for
+    # bit the oracle's.
+    rng = np.random.default_rng(77)
+    for shp in ((9, 37, 96), (4, 70, 256), (33, 5, 64), (2, 2, 32)):
+        for sdt in (np.uint8, np.int8):
+            a = rng.integers(0, 256, size=shp).astype(np.uint8)
+            a[rng.random(shp) < 0.3] = 0
+            a = a.view(sdt)
+            for it in (1, 2, 3):
+                got = run(clk, kernel, a, np.uint8, it)
+                want = oracle_iter(oracle, kernel, a, np.uint8, it)
+                assert np.array_equal(got, want), (kernel, shp, np.dtype(sdt), it)
