@@ -54,18 +54,19 @@ CONFIG1_SHAPE, CONFIG1_BLOBS, CONFIG1_SEED = (64, 256, 256), 200, 1
 L2_FLUSH_BYTES = 512 << 20  # written between timed calls whose data fits in L2 (129 MB)
 
 
-# DRAM bytes per voxel (read + write) of each filter's kernel, from one-kernel
-# ncu captures (dram__bytes_read.sum + dram__bytes_write.sum) of the build
+# DRAM bytes per voxel (read + write) of each filter's kernel from the ncu
+# launch list (dram__bytes_read.sum + dram__bytes_write.sum) of the build
 # named in TRAFFIC_SOURCE, on a 1024x1024x128 slab of the same stack (traffic
 # scales with the voxels).
-TRAFFIC_SOURCE = "ncu capture of the build before commit 3a9debb (earlier sphere-median network)"
+TRAFFIC_SOURCE = "ncu launch list of commit 30e1e1c, 1024x1024x128 slab, scaled to the stack"
 NCU_DRAM_BYTES_PER_VOXEL = {
-    "gaussian_blur s(3,3,1.5)": 5.86, "mean_box r(5,5,2)": 3.90, "minimum_box r(5,5,2)": 3.97,
-    "median_box r1": 3.73, "median_sphere r2": 3.73, "sobel_3d": 5.66,
+    "gaussian_blur s(3,3,1.5)": 5.75, "mean_box r(5,5,2)": 3.69, "minimum_box r(5,5,2)": 3.68,
+    "maximum_box r(5,5,2)": 3.67, "median_box r1": 3.70, "median_sphere r2": 3.70, "sobel_3d": 5.62,
+    "erode_sphere r1": 1.68, "erode_sphere r2": 1.75, "dilate_sphere r1": 1.68, "dilate_sphere r2": 1.75,
 }
 # The selection networks are bound by the min/max (ALU) pipe, not by DRAM:
-# its busy fraction from the same captures.
-NCU_ALU_PIPE_BUSY = {"median_box r1": 0.80, "median_sphere r2": 0.78}
+# its busy fraction from the one-kernel capture of the same build.
+NCU_ALU_PIPE_BUSY = {"median_sphere r2": 0.75}
 
 
 NOMINAL_HBM_GBS = 7900.0  # GB300 HBM3e, nominal (the measured copy peak is the roofline)

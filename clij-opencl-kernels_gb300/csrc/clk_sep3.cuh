@@ -589,10 +589,11 @@ template <class K> bool smem_ok(K kern, size_t smem) {
 
 // z-chunks: CLK_SEP3_CHUNKS in the environment fixes the count (tuning).
 // Otherwise about seven waves of CTAs (ctas_per_sm resident per SM), each
-// chunk at least 16 and 16*CZ planes long: the waves balance the SMs' loads
-// and the long chunks keep the 2CZ halo planes a small overhead (measured
-// on 1024 x 1024 x 256: minimum r5 0.47 ms with one chunk per tile, 0.35
-// with eight; the Gaussian cz = 5 best with two or three).
+// chunk long enough that its 2CZ halo planes stay a small overhead: at least
+// max(16, 24 CZ) planes while the tiles alone fill the SMs, max(8, 4 CZ) for
+// small images, where parallelism matters more (measured on 1024 x 1024 x
+// 256: minimum r5 0.47 ms with one chunk per tile, 0.29 with four to eight;
+// the Gaussian cz = 5 best with two chunks, 1.12 ms against 1.17 with three).
 inline int chunk_count(int tiles, int depth, int cz, int ctas_per_sm) {
   static const int forced = [] {
     const char* e = getenv("CLK_SEP3_CHUNKS");
@@ -604,7 +605,7 @@ inline int chunk_count(int tiles, int depth, int cz, int ctas_per_sm) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int64_t want = (int64_t)7 * sms * ctas_per_sm;
   int chunks = (int)std::max<int64_t>(1, (want + tiles / 2) / std::max(1, tiles));
-  const int minlen = std::max(16, 16 * cz);
+  const int minlen = tiles >= sms ? std::max(16, 24 * cz) : std::max(8, 4 * cz);
   chunks = std::min(chunks, std::max(1, depth / minlen));
   return chunks;
 }
