@@ -7,8 +7,10 @@
 // of a step run as concurrent graph nodes.  Images or steps without a
 // batched body (morphology, sobel, unusual radii or layouts) run their plain
 // calls inside the same graph.  The z-depth of a work item (zchunk) trades
-// load balance against halo re-reads; the autotuner times a few depths per
-// step on the real images and remembers the winner in a JSON cache.
+// load balance against halo re-reads, and integer-output separable images
+// can run on either tile body (register-window 64x32 or generic 64x16,
+// bit-identical); the autotuner times the depths (x bodies) per step on the
+// real images and remembers the winners in a JSON cache.
 #include <cuda_runtime.h>
 #include <sys/stat.h>
 
@@ -211,6 +213,7 @@ struct clk_batch {
   std::vector<clk::batch::SepDesc*> d_sep;
   std::vector<clk::batch::MedDesc*> d_med;
   std::vector<int> zchunk;
+  std::vector<char> generic;  // per step: integer-output separables on the 64x16 generic tiles
   cudaStream_t streams[4] = {};
   cudaEvent_t events[8] = {};
   cudaGraph_t graph = nullptr;
@@ -328,7 +331,10 @@ ImgStep plan_sep(clk_batch* b, int s, int i, SepDesc* d) {
     const bool s2_gauss = fast && R <= 12;
     const bool s2_gx = ints && opn == SEP_GAUSS && R <= 8 && in.dt == out.dt;  // exact order, as the plain path
     const bool s2_mmf = !ints && out.dt == CLK_F32 && (opn == SEP_MIN || opn == SEP_MAX) && R <= 8;
-    if (s2_int || s2_gauss || s2_gx || s2_mmf) {
+    // integer outputs are bit-identical on either body: the tuner may ask
+    // for the generic 64x16 tiles instead (b->generic[s])
+    const bool alt = s2_int || s2_gx;
+    if ((s2_int || s2_gauss || s2_gx || s2_mmf) && !(alt && b->generic[s])) {
       if (!batch_radius(R) || sep2_smem(opn, R, in.dt, cz) > 220 * 1024) return h;  // plain call keeps parity
       d->algo = A_SEP2;
       d->p2.cz = cz;
@@ -497,14 +503,74 @@ std::string step_key(const clk_batch* b, int s) {
   return k.str();
 }
 
+// Plan separable step s: every image's body (register-window or generic
+// tiles per b->generic[s], or a plain call) and one group (persistent
+// launch) per (radius, pixel type, body); replaces an earlier plan.
+clk_status plan_sep_step(clk_batch* b, int s) {
+  const int sop = sep_op_of(b->names[s]);
+  const int nimages = (int)b->src.size();
+  for (auto& g : b->groups[s])
+    if (g.d_items) cudaFree(g.d_items);
+  b->groups[s].clear();
+  if (b->d_sep[s]) cudaFree(b->d_sep[s]);
+  b->d_sep[s] = nullptr;
+  std::vector<SepDesc> hd(nimages);
+  std::map<std::tuple<int, int, bool>, int> gi;  // (R, dt, register-window body) -> group
+  for (int i = 0; i < nimages; ++i) {
+    b->how[s][i] = plan_sep(b, s, i, &hd[i]);
+    if (!b->how[s][i].algo) continue;
+    const bool s2 = b->how[s][i].algo == A_SEP2;
+    const auto key = std::make_tuple(b->how[s][i].R, b->src[i].dt, s2);
+    if (!gi.count(key)) {
+      Group g;
+      g.kernel = s2 ? batch_sep2_kernel(sop, std::get<0>(key), std::get<1>(key))
+                    : batch_sep_kernel(sop, std::get<0>(key), std::get<1>(key));
+      g.dt = std::get<1>(key);
+      if (!g.kernel) {
+        b->how[s][i].algo = 0;
+        continue;
+      }
+      gi[key] = (int)b->groups[s].size();
+      b->groups[s].push_back(g);
+    }
+    Group& g = b->groups[s][gi[key]];
+    g.imgs.push_back(i);
+    const ImgStep& h = b->how[s][i];
+    const size_t need = h.algo == A_SEP2
+                            ? sep2_smem(sop, h.R, b->src[i].dt, hd[i].p2.cz)
+                            : fused::fused_smem(hd[i].ft.c[0], hd[i].ft.c[1], hd[i].ft.c[2],
+                                                dtype_size(b->src[i].dt), dtype_size(b->dst[i].dt));
+    g.smem = std::max(g.smem, need);
+  }
+  if (cudaMalloc(&b->d_sep[s], nimages * sizeof(SepDesc)) != cudaSuccess ||
+      cudaMemcpy(b->d_sep[s], hd.data(), nimages * sizeof(SepDesc), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(CLK_OOM, "clk_batch_create: cannot allocate descriptors");
+  }
+  return CLK_OK;
+}
+
+// The tuner's choice per step, timed on the real images and cached under
+// the step's key: the depth of a work item (zchunk) and, for steps with
+// integer-output separable images, their tile body -- the register-window
+// 64x32 tiles or the generic 64x16 tiles (bit-identical results; key
+// "<step>|tile", 0 or 1).
 clk_status tune_step(clk_batch* b, int s, cudaStream_t st) {
   if (b->groups[s].empty()) {
     b->zchunk[s] = 0;
     return CLK_OK;
   }
-  const std::string key = step_key(b, s);
-  int best = 0;
+  const std::string key = step_key(b, s), tkey = key + "|tile";
+  bool two_bodies = false;
+  if (b->ops[s].kind == CLK_OP_SEPARABLE)
+    for (size_t i = 0; i < b->src.size(); ++i)
+      two_bodies |= b->how[s][i].algo == A_SEP2 && b->dst[i].dt != CLK_F32;
+  int best = 0, tile = 0;
   if (g_tune.get(key, &best)) {
+    if (two_bodies && g_tune.get(tkey, &tile) && tile != b->generic[s]) {
+      b->generic[s] = (char)tile;
+      if (clk_status r = plan_sep_step(b, s)) return r;
+    }
     b->zchunk[s] = best;
     return upload_step(b, s, best, st);
   }
@@ -514,28 +580,39 @@ clk_status tune_step(clk_batch* b, int s, cudaStream_t st) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   clk_status res = CLK_OK;
-  for (int zc : cands) {
-    if ((res = upload_step(b, s, zc, st))) break;
-    for (const Group& g : b->groups[s])  // warm-up
-      if ((res = launch_group(b, s, g, st))) break;
-    float ms_min = 1e30f;
-    for (int rep = 0; rep < 3 && res == CLK_OK; ++rep) {
-      cudaEventRecord(e0, st);
-      for (const Group& g : b->groups[s])
-        if ((res = launch_group(b, s, g, st))) break;
-      cudaEventRecord(e1, st);
-      cudaEventSynchronize(e1);
-      float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
-      ms_min = std::min(ms_min, ms);
+  for (int t = 0; t < (two_bodies ? 2 : 1) && res == CLK_OK; ++t) {
+    if (t != b->generic[s]) {
+      b->generic[s] = (char)t;
+      if ((res = plan_sep_step(b, s))) break;
     }
-    if (res) break;
-    if (ms_min < best_ms) best_ms = ms_min, best = zc;
+    for (int zc : cands) {
+      if ((res = upload_step(b, s, zc, st))) break;
+      for (const Group& g : b->groups[s])  // warm-up
+        if ((res = launch_group(b, s, g, st))) break;
+      float ms_min = 1e30f;
+      for (int rep = 0; rep < 3 && res == CLK_OK; ++rep) {
+        cudaEventRecord(e0, st);
+        for (const Group& g : b->groups[s])
+          if ((res = launch_group(b, s, g, st))) break;
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms_min = std::min(ms_min, ms);
+      }
+      if (res) break;
+      if (ms_min < best_ms) best_ms = ms_min, best = zc, tile = t;
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (res) return res;
+  if (tile != b->generic[s]) {
+    b->generic[s] = (char)tile;
+    if ((res = plan_sep_step(b, s))) return res;
+  }
   g_tune.put(key, best);
+  if (two_bodies) g_tune.put(tkey, tile);
   b->zchunk[s] = best;
   return upload_step(b, s, best, st);
 }
@@ -671,44 +748,13 @@ clk_status clk_batch_create(const clk_op* ops, int32_t nops, const clk_image* sr
   b->d_sep.assign(nops, nullptr);
   b->d_med.assign(nops, nullptr);
   b->zchunk.assign(nops, 0);
+  b->generic.assign(nops, 0);
   clk_status res = CLK_OK;
   for (int s = 0; s < nops && res == CLK_OK; ++s) {
     const int sop = sep_op_of(b->names[s]);
     const bool med = b->names[s] == "median_box" || b->names[s] == "median_sphere";
     if (b->ops[s].kind == CLK_OP_SEPARABLE && sop >= 0) {
-      std::vector<SepDesc> hd(nimages);
-      std::map<std::tuple<int, int, bool>, int> gi;  // (R, dt, register-window body) -> group
-      for (int i = 0; i < nimages; ++i) {
-        b->how[s][i] = plan_sep(b, s, i, &hd[i]);
-        if (!b->how[s][i].algo) continue;
-        const bool s2 = b->how[s][i].algo == A_SEP2;
-        const auto key = std::make_tuple(b->how[s][i].R, b->src[i].dt, s2);
-        if (!gi.count(key)) {
-          Group g;
-          g.kernel = s2 ? batch_sep2_kernel(sop, std::get<0>(key), std::get<1>(key))
-                        : batch_sep_kernel(sop, std::get<0>(key), std::get<1>(key));
-          g.dt = std::get<1>(key);
-          if (!g.kernel) {
-            b->how[s][i].algo = 0;
-            continue;
-          }
-          gi[key] = (int)b->groups[s].size();
-          b->groups[s].push_back(g);
-        }
-        Group& g = b->groups[s][gi[key]];
-        g.imgs.push_back(i);
-        const ImgStep& h = b->how[s][i];
-        const size_t need = h.algo == A_SEP2
-                                ? sep2_smem(sop, h.R, b->src[i].dt, hd[i].p2.cz)
-                                : fused::fused_smem(hd[i].ft.c[0], hd[i].ft.c[1], hd[i].ft.c[2],
-                                                    dtype_size(b->src[i].dt), dtype_size(b->dst[i].dt));
-        g.smem = std::max(g.smem, need);
-      }
-      if (cudaMalloc(&b->d_sep[s], nimages * sizeof(SepDesc)) != cudaSuccess ||
-          cudaMemcpy(b->d_sep[s], hd.data(), nimages * sizeof(SepDesc), cudaMemcpyHostToDevice) != cudaSuccess) {
-        cudaGetLastError();
-        res = fail(CLK_OOM, "clk_batch_create: cannot allocate descriptors");
-      }
+      res = plan_sep_step(b, s);
     } else if (b->ops[s].kind == CLK_OP_KERNEL && med) {
       std::vector<MedDesc> hd(nimages);
       std::map<int, int> gi;
@@ -744,7 +790,6 @@ clk_status clk_batch_create(const clk_op* ops, int32_t nops, const clk_image* sr
   // capture the pipeline
   if (res == CLK_OK) {
     const uint64_t before = clk_launch_count();
-    cudaStream_t cap = b->streams[0];
     cudaStream_t cs = nullptr;
     cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
@@ -759,7 +804,6 @@ clk_status clk_batch_create(const clk_op* ops, int32_t nops, const clk_image* sr
         res = check_launch("batch graph instantiate");
     }
     cudaGetLastError();
-    (void)cap;
     if (cs) cudaStreamDestroy(cs);
     uncount_launches(clk_launch_count() - before);  // capture is not execution
     if (res == CLK_OK) {

@@ -78,6 +78,13 @@ def test_batched_equals_plain(clk, chain, tmp_path, monkeypatch):
     for k, (g, w) in enumerate(zip(got, want)):
         assert g.tobytes() == w.tobytes(), (chain, k, imgs[k].shape, imgs[k].dtype)
     assert (tmp_path / "tune.json").exists()
+    # the tuner chose, per step, a work-item depth and, for the integer
+    # separable steps, a tile body (0: register-window 64x32, 1: generic 64x16)
+    import json
+    tune = json.loads((tmp_path / "tune.json").read_text())
+    tiles = {k: v for k, v in tune.items() if k.endswith("|tile")}
+    assert tiles and all(v in (0, 1) for v in tiles.values()), tune
+    assert all(k[: -len("|tile")] in tune for k in tiles), tune
 
 
 def test_batched_tophat_matches_oracle_on_integer_images(clk, oracle, tmp_path, monkeypatch):
