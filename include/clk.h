@@ -201,8 +201,10 @@ clk_status clk_morphology(const char* kernel_name, const clk_image* dst,
  * of uneven shape and pixel type.  Each step runs as ONE persistent launch
  * over a work list of tiles of all images (pixel type dispatched per tile),
  * the pipeline is captured once as a CUDA graph, and the z-depth of a work
- * item is picked by an autotuner whose choices persist in a JSON cache
- * (env CLK_AUTOTUNE_CACHE, default $HOME/.cache/clk_gb300/autotune.json).
+ * item and, for integer-output separable steps, the tile body (64x32
+ * register-window or 64x16 generic tiles) are picked by an autotuner whose
+ * choices persist in a JSON cache (env CLK_AUTOTUNE_CACHE, default
+ * $HOME/.cache/clk_gb300/autotune.json).
  * Results equal per-image plain calls bit for bit.
  * Replaces: the host loop that enqueues every kernel per image (CLIc /
  *   pyclesperanto), which the reference leaves to its callers.
