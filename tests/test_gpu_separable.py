@@ -143,3 +143,39 @@ def test_ragged_tile_grid(clk, oracle):
     for N, s in (((19, 19, 11), (3.0, 3.0, 1.5)), ((7, 7, 5), (1.0, 1.0, 0.6))):
         val, scale = oracle.fp64("gaussian_blur_separable_3d", a, N, s)
         assert close(run(clk, "gaussian_blur_separable_3d", a, np.float32, N, s), val, scale), N
+
+
+@pytest.mark.parametrize("kernel", ["minimum_separable_3d", "maximum_separable_3d", "mean_separable_3d"])
+def test_register_ring_kernels_every_z_radius(clk, oracle, kernel):
+    # 16-bit pixels with x extents a multiple of 8 take the register-ring
+    # kernels for Z radii 0..3 (every XY radius 1..8): tiny and one-plane
+    # stacks, one-row images, tile-ragged extents, extremes of the pixel
+    # range (signed and unsigned), against the oracle bit for bit
+    rng = np.random.default_rng(41)
+    for dt in (np.uint16, np.int16):
+        for shp in ((7, 45, 72), (2, 3, 8), (1, 33, 64), (9, 1, 136), (5, 70, 200)):
+            a = random_image(rng, shp, dt)
+            info = np.iinfo(dt)
+            a.flat[:: 97] = info.max
+            a.flat[5:: 89] = info.min
+            for R in range(1, 9):
+                for rz in range(0, 4):
+                    N = (2 * R + 1, 2 * R + 1, 2 * rz + 1)
+                    want = oracle.separable(kernel, a, dt, N, (R, R, rz))
+                    got = run(clk, kernel, a, dt, N, (R, R, rz))
+                    assert np.array_equal(got, want), (kernel, shp, np.dtype(dt), N)
+
+
+def test_register_ring_gaussian_every_z_radius(clk, oracle):
+    # u16 -> f32 Gaussians on the register-ring kernel: XY radius 1..12, Z
+    # radius 0..6, within the stated tolerance of the FP64 oracle
+    rng = np.random.default_rng(42)
+    for shp in ((14, 45, 72), (1, 33, 64), (3, 2, 16), (20, 70, 200)):
+        a = random_image(rng, shp, np.uint16)
+        for R in (1, 2, 4, 7, 10, 12):
+            for cz in range(0, 7):
+                N = (2 * R + 1, 2 * R + 1, 2 * cz + 1)
+                s = (R / 3.0, R / 3.0, cz / 3.0 if cz else 0.0)
+                val, scale = oracle.fp64("gaussian_blur_separable_3d", a, N, s)
+                got = run(clk, "gaussian_blur_separable_3d", a, np.float32, N, s)
+                assert close(got, val, scale), (shp, N, s)
