@@ -18,6 +18,7 @@
 //     multiply-high equal to trunc(fl(S / N)), |S| < 2^24, N < 256).
 //   Gaussian to float: taps pre-divided by their sum, fma.rn.f32x2; within
 //     the float tolerance of the FP64 oracle.
+#include <cstring>
 #include <type_traits>
 
 #include "clk_common.cuh"
@@ -34,7 +35,9 @@ constexpr int TC = 64;   // columns per tile across the axis (32 lane pairs)
 constexpr int kMaxR = 127;
 
 struct Params {
-  float w[2 * kMaxR + 1];  // Gaussian: normalised taps of v = -R..R
+  // Gaussian: normalised taps of v = -R..R, each as the f32x2 pair (w, w)
+  // that the packed FMA takes straight from the parameter space
+  uint64_t w2[2 * kMaxR + 1];
   uint32_t mrecip;         // mean: ceil(2^32 / N)
   int R;
 };
@@ -119,8 +122,10 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
   };
 
   // stage lines l0 - R .. l0 - R + NLS - 1 (clamped) x the tile's columns
-  // AXIS 0: sm[c * NP + l] (odd pitch NP: the lanes' rows hit distinct
-  // banks); AXIS 1/2: sm[l * TC + c] (lane pairs adjacent)
+  // AXIS 0: columns c and c + 32 (a thread's two rows) interleaved,
+  // sm[((c % 32) * NP + l) * 2 + c / 32], so that one 8-byte read fetches
+  // both lanes (odd pitch NP: a warp's reads hit distinct banks); AXIS 1/2:
+  // sm[l * TC + c] (lane pairs adjacent)
   // Loads are batched U deep so that each thread has U in flight.
   constexpr int U = 8;
   const int NP = NLS | 1;
@@ -132,7 +137,10 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
 #pragma unroll
       for (int u = 0; u < U; ++u) v[u] = (T)__ldg(src + at(ll, min(c0 + warp + 8 * u, C - 1)));
 #pragma unroll
-      for (int u = 0; u < U; ++u) sm[(warp + 8 * u) * NP + l] = v[u];
+      for (int u = 0; u < U; ++u) {
+        const int c = warp + 8 * u;
+        sm[((c & 31) * NP + l) * 2 + (c >> 5)] = v[u];
+      }
     }
   } else {
     const int total = NLS * TC;  // element i = (line i / 64, column i % 64) = sm[i]
@@ -156,10 +164,11 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
   const int ca = AXIS == 0 ? lane : 2 * lane, cb = AXIS == 0 ? lane + 32 : 2 * lane + 1;
   auto get = [&](int l) -> Lane<OP, T> {
     T a, b;
-    if constexpr (AXIS == 0) {
-      a = sm[ca * NP + l], b = sm[cb * NP + l];
+    typedef typename std::conditional<std::is_same<T, float>::value, float2, int2>::type P2;
+    if constexpr (AXIS == 0) {  // rows ca, cb = ca + 32, interleaved: one 8-byte read
+      const P2 v = *reinterpret_cast<const P2*>(sm + (ca * NP + l) * 2);
+      a = v.x, b = v.y;
     } else {  // the adjacent pair as one 8-byte read
-      typedef typename std::conditional<std::is_same<T, float>::value, float2, int2>::type P2;
       const P2 v = *reinterpret_cast<const P2*>(sm + l * TC + ca);
       a = v.x, b = v.y;
     }
@@ -267,10 +276,7 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
       const int k = kk + t;
       if (k <= 2 * R) {
         uint64_t wk = 0;
-        if constexpr (OP == GAUSS) {
-          const float w = p.w[k];
-          wk = f2(w, w);
-        }
+        if constexpr (OP == GAUSS) wk = p.w2[k];
 #pragma unroll
         for (int j = 0; j < M; ++j) {
           const Lane<OP, T>& v = win[(j + t) % M];
@@ -382,7 +388,12 @@ clk_status line_pass(SepOp op, const Image& dst, const Image& src, int axis, con
   if (op == SEP_GAUSS) {
     double s = 0;
     for (int v = 0; v <= 2 * taps.c; ++v) s += taps.h[v];
-    for (int v = 0; v <= 2 * taps.c; ++v) p.w[v] = (float)(taps.h[v] / s);
+    for (int v = 0; v <= 2 * taps.c; ++v) {
+      const float w = (float)(taps.h[v] / s);
+      uint32_t u;
+      memcpy(&u, &w, 4);
+      p.w2[v] = (uint64_t)u | ((uint64_t)u << 32);
+    }
   } else if (op == SEP_MEAN) {
     const uint64_t n = 2 * (uint64_t)taps.c + 1;
     p.mrecip = (uint32_t)((((uint64_t)1 << 32) + n - 1) / n);
