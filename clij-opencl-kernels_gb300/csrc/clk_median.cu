@@ -18,7 +18,9 @@
 //  * box: the merge of planes z and z+1 (ranks 4..13) serves the outputs at
 //    z and z+1; each then needs one rank-9 selection against the third plane;
 //    8/16-bit pixels also pair rows y and y+1, whose blocks share two sorted
-//    rows (k_median_box27_yp);
+//    rows (k_median_box27_yp); 16-bit images whose rows are whole 16-byte
+//    vectors stage each plane tile in shared memory with cp.async, two
+//    planes ahead, and read the rows from there (k_median_box27_st);
 //  * sphere (8/16-bit): likewise the merge of planes z and z+1 (16 ranks)
 //    serves z and z+1, each adding its other plane's block and six singles;
 //  * the next z-pair's planes are loaded before the current pair's networks.
@@ -54,6 +56,16 @@ bool ypair_enabled() {
   return on;
 }
 
+// CLK_MEDIAN_STAGED=0 in the environment keeps the medians' rows on global
+// loads (A/B timing)
+bool staged_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("CLK_MEDIAN_STAGED");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 template <class T, bool ODD> clk_status launch(Shape sh, const Image& dst, const Image& src, cudaStream_t st) {
   const dim3 block(BX * BY);
   const int tx = ((src.w + 1) / 2 + BX - 1) / BX, ty = (src.h + BY - 1) / BY;
@@ -69,8 +81,16 @@ template <class T, bool ODD> clk_status launch(Shape sh, const Image& dst, const
     zchunk += zchunk & 1;  // outputs come in z pairs
     const dim3 grid(tx, ty, (src.d + zchunk - 1) / zchunk);
     bool done = false;
+    if constexpr (sizeof(T) == 2 && !ODD) {  // planes staged in shared memory: 16-bit rows of whole vectors
+      if (sh == BOX27 && ypair_enabled() && staged_enabled() && src.w % 8 == 0 &&
+          ((uintptr_t)src.ptr | (uintptr_t)dst.ptr) % 16 == 0) {
+        const dim3 gy(tx, (src.h + BYP - 1) / BYP, grid.z);
+        k_median_box27_st<T><<<gy, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);
+        done = true;
+      }
+    }
     if constexpr (sizeof(T) <= 2) {  // y pairs: 8/16-bit lanes (float keys would spill)
-      if (sh == BOX27 && ypair_enabled()) {
+      if (!done && sh == BOX27 && ypair_enabled()) {
         const dim3 gy(tx, (src.h + BYP - 1) / BYP, grid.z);
         k_median_box27_yp<T, ODD><<<gy, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d,
                                                         zchunk);

@@ -310,6 +310,130 @@ __device__ __forceinline__ void box27_ypair_tile(const T* __restrict__ src, T* _
   }
 }
 
+// The y-pair box median with each plane staged in shared memory (16-bit
+// pixels, rows of whole 16-byte vectors): a CTA copies the clamped rows
+// y0-1 .. y0+BYP of its 64 + 16 columns with cp.async, two planes ahead,
+// into a ring of four plane buffers; tiles at the x border fill their
+// outside vectors with the row's edge pixel, so a thread reads its words
+// (x-2, x-1), (x, x+1), (x+2, x+3) from shared memory without clamping.
+// The rows' loads then wait on shared memory instead of L1 / L2.
+constexpr int SMR = BYP + 2;                 // staged rows
+constexpr int SMW = 2 * BX + 16;             // staged pixels per row (8 each side)
+constexpr int SMV = SMW / 8;                 // 16-byte vectors per staged row
+static_assert(SMR * SMV <= BX * BY, "one staging vector per thread");
+
+__device__ __forceinline__ void med_cp_async16(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc)
+               : "memory");
+}
+
+template <class T>
+__device__ __forceinline__ void stage_plane_async(const T* plane, int x0, int y0, int W, int H, uint16_t* buf) {
+  const int t = threadIdx.x;
+  if (t < SMR * SMV) {
+    const int r = t / SMV, v = t - r * SMV;
+    const int gx = x0 - 8 + 8 * v;
+    if (gx >= 0 && gx < W)  // vectors outside the row are filled once landed
+      med_cp_async16(buf + r * SMW + 8 * v, plane + (int64_t)clampi(y0 - 1 + r, H - 1) * W + gx);
+  }
+}
+__device__ __forceinline__ void fill_plane(uint16_t* buf, int x0, int W) {
+  const int t = threadIdx.x;
+  if (t < SMR * SMV) {
+    const int r = t / SMV, v = t - r * SMV;
+    const int gx = x0 - 8 + 8 * v;
+    if (gx < 0 || gx >= W) {
+      const uint32_t e = (uint32_t)buf[r * SMW + (gx < 0 ? 0 : W - 1) - (x0 - 8)] * 0x10001u;
+      *reinterpret_cast<uint4*>(buf + r * SMW + 8 * v) = make_uint4(e, e, e, e);
+    }
+  }
+}
+// rows y-1 .. y+2 of a staged plane as the lane words a, b, c of each row
+template <class V> __device__ __forceinline__ void rows4_smem(const uint16_t* buf, int px, int py, V (&q)[12]) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(buf + (2 * py + r) * SMW) + px + 3;
+    const uint32_t l = w[0], b = w[1], c = w[2];
+    q[3 * r] = V{__byte_perm(l, b, 0x5432)};
+    q[3 * r + 1] = V{b};
+    q[3 * r + 2] = V{__byte_perm(b, c, 0x5432)};
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void box27_staged_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int D,
+                                                  int zchunk, int bx, int by, int bz) {
+  static_assert(sizeof(T) == 2, "16-bit pixels");
+  using V = typename Px<T>::V;
+  __shared__ __align__(16) uint16_t buf[4][SMR * SMW];
+  const int px = (int)threadIdx.x % BX, py = (int)threadIdx.x / BX;
+  const int x0 = bx * 2 * BX, y0 = by * BYP;
+  const int x = x0 + 2 * px, y = y0 + 2 * py;
+  const bool act = x < W && y < H, two = y + 1 < H;
+  const bool xb = x0 - 8 < 0 || x0 + SMW - 8 > W;  // outside vectors to fill
+  const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+  auto pl = [&](int z) { return src + (int64_t)clampi(z, D - 1) * plane; };
+  V am1[9], bm1[9], a0[9], b0[9];  // sorted blocks (row y: a, row y+1: b) of planes zo-1, zo
+  V q1[12], q2[12];
+  stage_plane_async(pl(z0 - 1), x0, y0, W, H, buf[0]);
+  stage_plane_async(pl(z0), x0, y0, W, H, buf[1]);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  __syncthreads();
+  if (xb) {
+    fill_plane(buf[0], x0, W);
+    fill_plane(buf[1], x0, W);
+    __syncthreads();
+  }
+  rows4_smem(buf[0], px, py, q1);
+  blocks_ypair(q1, am1, bm1);
+  rows4_smem(buf[1], px, py, q1);
+  blocks_ypair(q1, a0, b0);
+  stage_plane_async(pl(z0 + 1), x0, y0, W, H, buf[2]);
+  stage_plane_async(pl(z0 + 2), x0, y0, W, H, buf[3]);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  int slot = 2;  // buffers of planes zo+1, zo+2
+  for (int zo = z0; zo < z1; zo += 2) {
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();  // planes zo+1, zo+2 landed; the other pair's last reads are done
+    if (xb) {
+      fill_plane(buf[slot], x0, W);
+      fill_plane(buf[slot + 1], x0, W);
+      __syncthreads();
+    }
+    const int nslot = slot ^ 2;
+    if (zo + 2 < z1) {
+      stage_plane_async(pl(zo + 3), x0, y0, W, H, buf[nslot]);
+      stage_plane_async(pl(zo + 4), x0, y0, W, H, buf[nslot + 1]);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    rows4_smem(buf[slot], px, py, q1);
+    rows4_smem(buf[slot + 1], px, py, q2);
+    V a1[9], b1[9], a2[9], b2[9];
+    blocks_ypair(q1, a1, b1);
+    blocks_ypair(q2, a2, b2);
+    T* o0 = dst + (int64_t)zo * plane + (int64_t)y * W;
+    if (act) {
+      V m[10];
+      merge_mid(a0, a1, m);
+      store_pair<T, false>(o0, x, W, final27(m, am1));
+      if (zo + 1 < z1) store_pair<T, false>(o0 + plane, x, W, final27(m, a2));
+    }
+    if (act && two) {
+      V m[10];
+      merge_mid(b0, b1, m);
+      store_pair<T, false>(o0 + W, x, W, final27(m, bm1));
+      if (zo + 1 < z1) store_pair<T, false>(o0 + plane + W, x, W, final27(m, b2));
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) am1[k] = a1[k], bm1[k] = b1[k], a0[k] = a2[k], b0[k] = b2[k];
+    slot = nslot;
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 // median_sphere_3d with Nx = Ny = Nz = 5: per output the 3x3 blocks of
 // planes z-1, z, z+1, the four voxels at distance 2 in plane z and the two
 // at distance 2 along z (33 = 9 + 9 + 9 + 4 + 2).
@@ -461,6 +585,11 @@ template <class T, bool ODD>
 __global__ void __launch_bounds__(BX * BY, 2) k_median_box27_yp(const T* __restrict__ src, T* __restrict__ dst,
                                                                  int W, int H, int D, int zchunk) {
   box27_ypair_tile<T, ODD>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+template <class T>
+__global__ void __launch_bounds__(BX * BY, 2) k_median_box27_st(const T* __restrict__ src, T* __restrict__ dst,
+                                                                 int W, int H, int D, int zchunk) {
+  box27_staged_tile<T>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 // 16-bit pixels fit the sphere network in 64 registers without spilling:
 // four CTAs per SM instead of three

@@ -51,14 +51,14 @@ using sep2::f2_pack;
 using sep2::f2_unpack;
 
 enum Op { MIN = 0, MAX = 1, MEAN = 2, GAUSS = 3 };
-constexpr int TX = 64, TY = 32;
+constexpr int TX = 64;  // output columns per tile (32 column pairs: one warp)
 
 // Launch shape: NT threads; the Y/Z pass gives a thread a column pair x
 // SEGY rows (threads beyond 32 x TY/SEGY sit out the Y/Z pass); an X task is
 // MX outputs of a row pair (the Gaussian: 8); MINB CTAs per SM for the
 // register budget.
-template <int NT_, int SEGY_, int MX_, int MINB_> struct Cfg {
-  static constexpr int NT = NT_, SEGY = SEGY_, MX = MX_, MINB = MINB_;
+template <int NT_, int SEGY_, int MX_, int MINB_, int TY_ = 32> struct Cfg {
+  static constexpr int NT = NT_, SEGY = SEGY_, MX = MX_, MINB = MINB_, TY = TY_;  // TY: output rows per tile
 };
 // instantiated radii: XY radius 1..kMaxRInt (min / max / mean) or
 // 1..kMaxRGauss, Z radius 0..kMaxCz*; other radii take the generic fused
@@ -84,7 +84,7 @@ template <int N, class F> __device__ __forceinline__ void static_for(F&& f) {
 }
 
 template <int OP, int R, int CZ, class C> struct Geo {
-  static constexpr int NT = C::NT;
+  static constexpr int NT = C::NT, TY = C::TY;
   static constexpr int MX = OP == GAUSS ? 8 : C::MX;  // outputs of an X task
   static constexpr int RA = rup(R, 8);         // staged margin left and right (whole vectors)
   static constexpr int SW = TX + 2 * RA;       // staged columns
@@ -183,10 +183,11 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
     k_sep3(const S* __restrict__ src, void* __restrict__ dstv, int W, int H, int Dz, int zchunk,
            const __grid_constant__ P3 p) {
   using G = Geo<OP, R, CZ, C>;
-  constexpr int NT = C::NT, SEGY = C::SEGY, MX = G::MX;
+  constexpr int NT = C::NT, SEGY = C::SEGY, MX = G::MX, TY = C::TY;
   constexpr bool SG = std::is_signed<S>::value;
   constexpr int NZ = G::NZ;
   static_assert(G::XTASKS <= NT, "one X task per thread");
+  static_assert(NT / 32 * SEGY >= TY, "the Y tasks cover the tile");
   extern __shared__ __align__(128) unsigned char smem[];
   // byte offsets of the buffers in shared memory
   constexpr uint32_t RAW0 = 0, CV0 = G::NRAW * G::RAW_BYTES, XS0 = CV0 + 2 * G::CV_BYTES;
@@ -623,7 +624,7 @@ clk_status launch(const Image& dst, const Image& src, const P3& p, cudaStream_t 
   using G = Geo<OP, R, CZ, C>;
   auto kern = k_sep3<S, OP, R, CZ, C>;
   if (!smem_ok(kern, G::SMEM)) return CLK_UNSUPPORTED_DTYPE;
-  const int tx = (dst.w + TX - 1) / TX, ty = (dst.h + TY - 1) / TY;
+  const int tx = (dst.w + TX - 1) / TX, ty = (dst.h + C::TY - 1) / C::TY;
   if (chunks <= 0) chunks = chunk_count(tx * ty, dst.d, CZ, C::MINB);
   const int zchunk = (dst.d + chunks - 1) / chunks;
   const dim3 grid(tx, ty, (dst.d + zchunk - 1) / zchunk);
