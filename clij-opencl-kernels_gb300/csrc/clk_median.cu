@@ -23,6 +23,8 @@
 //    planes ahead, and read the rows from there (k_median_box27_st);
 //  * sphere (8/16-bit): likewise the merge of planes z and z+1 (16 ranks)
 //    serves z and z+1, each adding its other plane's block and six singles;
+//    16-bit rows of whole vectors read staged planes from a ring of eight in
+//    shared memory (k_median_sphere33_st);
 //  * the next z-pair's planes are loaded before the current pair's networks.
 // Borders clamp exactly as the reference's reads do.
 #include <cstdlib>
@@ -86,6 +88,10 @@ template <class T, bool ODD> clk_status launch(Shape sh, const Image& dst, const
           ((uintptr_t)src.ptr | (uintptr_t)dst.ptr) % 16 == 0) {
         const dim3 gy(tx, (src.h + BYP - 1) / BYP, grid.z);
         k_median_box27_st<T><<<gy, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);
+        done = true;
+      } else if (sh == SPHERE33 && staged_enabled() && src.w % 8 == 0 &&
+                 ((uintptr_t)src.ptr | (uintptr_t)dst.ptr) % 16 == 0) {
+        k_median_sphere33_st<T><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);
         done = true;
       }
     }

@@ -320,7 +320,6 @@ __device__ __forceinline__ void box27_ypair_tile(const T* __restrict__ src, T* _
 constexpr int SMR = BYP + 2;                 // staged rows
 constexpr int SMW = 2 * BX + 16;             // staged pixels per row (8 each side)
 constexpr int SMV = SMW / 8;                 // 16-byte vectors per staged row
-static_assert(SMR * SMV <= BX * BY, "one staging vector per thread");
 
 __device__ __forceinline__ void med_cp_async16(void* sdst, const void* gsrc) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
@@ -328,19 +327,21 @@ __device__ __forceinline__ void med_cp_async16(void* sdst, const void* gsrc) {
                : "memory");
 }
 
-template <class T>
+// rows y0-HY .. y0-HY+NR-1 (clamped) of a plane, one vector per thread
+template <int NR, int HY, class T>
 __device__ __forceinline__ void stage_plane_async(const T* plane, int x0, int y0, int W, int H, uint16_t* buf) {
+  static_assert(NR * SMV <= BX * BY, "one staging vector per thread");
   const int t = threadIdx.x;
-  if (t < SMR * SMV) {
+  if (t < NR * SMV) {
     const int r = t / SMV, v = t - r * SMV;
     const int gx = x0 - 8 + 8 * v;
     if (gx >= 0 && gx < W)  // vectors outside the row are filled once landed
-      med_cp_async16(buf + r * SMW + 8 * v, plane + (int64_t)clampi(y0 - 1 + r, H - 1) * W + gx);
+      med_cp_async16(buf + r * SMW + 8 * v, plane + (int64_t)clampi(y0 - HY + r, H - 1) * W + gx);
   }
 }
-__device__ __forceinline__ void fill_plane(uint16_t* buf, int x0, int W) {
+template <int NR> __device__ __forceinline__ void fill_plane(uint16_t* buf, int x0, int W) {
   const int t = threadIdx.x;
-  if (t < SMR * SMV) {
+  if (t < NR * SMV) {
     const int r = t / SMV, v = t - r * SMV;
     const int gx = x0 - 8 + 8 * v;
     if (gx < 0 || gx >= W) {
@@ -377,36 +378,36 @@ __device__ __forceinline__ void box27_staged_tile(const T* __restrict__ src, T* 
   auto pl = [&](int z) { return src + (int64_t)clampi(z, D - 1) * plane; };
   V am1[9], bm1[9], a0[9], b0[9];  // sorted blocks (row y: a, row y+1: b) of planes zo-1, zo
   V q1[12], q2[12];
-  stage_plane_async(pl(z0 - 1), x0, y0, W, H, buf[0]);
-  stage_plane_async(pl(z0), x0, y0, W, H, buf[1]);
+  stage_plane_async<SMR, 1>(pl(z0 - 1), x0, y0, W, H, buf[0]);
+  stage_plane_async<SMR, 1>(pl(z0), x0, y0, W, H, buf[1]);
   asm volatile("cp.async.commit_group;" ::: "memory");
   asm volatile("cp.async.wait_group 0;" ::: "memory");
   __syncthreads();
   if (xb) {
-    fill_plane(buf[0], x0, W);
-    fill_plane(buf[1], x0, W);
+    fill_plane<SMR>(buf[0], x0, W);
+    fill_plane<SMR>(buf[1], x0, W);
     __syncthreads();
   }
   rows4_smem(buf[0], px, py, q1);
   blocks_ypair(q1, am1, bm1);
   rows4_smem(buf[1], px, py, q1);
   blocks_ypair(q1, a0, b0);
-  stage_plane_async(pl(z0 + 1), x0, y0, W, H, buf[2]);
-  stage_plane_async(pl(z0 + 2), x0, y0, W, H, buf[3]);
+  stage_plane_async<SMR, 1>(pl(z0 + 1), x0, y0, W, H, buf[2]);
+  stage_plane_async<SMR, 1>(pl(z0 + 2), x0, y0, W, H, buf[3]);
   asm volatile("cp.async.commit_group;" ::: "memory");
   int slot = 2;  // buffers of planes zo+1, zo+2
   for (int zo = z0; zo < z1; zo += 2) {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();  // planes zo+1, zo+2 landed; the other pair's last reads are done
     if (xb) {
-      fill_plane(buf[slot], x0, W);
-      fill_plane(buf[slot + 1], x0, W);
+      fill_plane<SMR>(buf[slot], x0, W);
+      fill_plane<SMR>(buf[slot + 1], x0, W);
       __syncthreads();
     }
     const int nslot = slot ^ 2;
     if (zo + 2 < z1) {
-      stage_plane_async(pl(zo + 3), x0, y0, W, H, buf[nslot]);
-      stage_plane_async(pl(zo + 4), x0, y0, W, H, buf[nslot + 1]);
+      stage_plane_async<SMR, 1>(pl(zo + 3), x0, y0, W, H, buf[nslot]);
+      stage_plane_async<SMR, 1>(pl(zo + 4), x0, y0, W, H, buf[nslot + 1]);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
     rows4_smem(buf[slot], px, py, q1);
@@ -554,6 +555,121 @@ __device__ __forceinline__ void sphere33_pair_tile(const T* __restrict__ src, T*
   }
 }
 
+// The z-pair sphere median for 16-bit images whose rows are whole 16-byte
+// vectors, its planes staged in shared memory: rows y0-2 .. y0+BY+1 of the
+// tile's 64 + 16 columns (outside vectors filled with the row's edge pixel),
+// in a ring of eight plane buffers.  The pair (zo, zo+1) reads planes zo-1 ..
+// zo+4 while zo+5 and zo+6 land; every read is then a shared-memory word at a
+// fixed offset, with no clamping and no row addressing per load.
+constexpr int SPR = BY + 4;  // staged rows of a sphere tile
+template <class T>
+__device__ __forceinline__ void sphere33_staged_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H,
+                                                     int D, int zchunk, int bx, int by, int bz) {
+  static_assert(sizeof(T) == 2, "16-bit pixels");
+  using V = typename Px<T>::V;
+  __shared__ __align__(16) uint16_t buf[8][SPR * SMW];
+  const int px = (int)threadIdx.x % BX, py = (int)threadIdx.x / BX;
+  const int x0 = bx * 2 * BX, y0 = by * BY;
+  const int x = x0 + 2 * px, y = y0 + py;
+  const bool act = x < W && y < H;
+  const bool xb = x0 - 8 < 0 || x0 + SMW - 8 > W;  // outside vectors to fill
+  const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+  auto slot = [&](int z) { return buf[(z - z0 + 2) & 7]; };  // planes z0-2 .. z1+4
+  auto stage = [&](int z) { stage_plane_async<SPR, 2>(src + (int64_t)clampi(z, D - 1) * plane, x0, y0, W, H, slot(z)); };
+  // the words (x-2, x-1), (x, x+1), (x+2, x+3) of row y+dy of plane z
+  auto row = [&](int z, int dy) {
+    return reinterpret_cast<const uint32_t*>(slot(z) + (py + 2 + dy) * SMW) + px + 3;
+  };
+  auto blk = [&](int z, V (&p)[9]) {
+    V w[9];
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy) {
+      const uint32_t* r = row(z, dy);
+      const uint32_t l = r[0], b = r[1], c = r[2];
+      w[dy + 1] = V{__byte_perm(l, b, 0x5432)};
+      w[dy + 4] = V{b};
+      w[dy + 7] = V{__byte_perm(b, c, 0x5432)};
+    }
+    sort9(w, p);
+  };
+  auto centre = [&](int z) { return V{row(z, 0)[1]}; };
+  auto singles = [&](int z, V (&s)[6]) {  // x -+ 2 and y -+ 2 in plane z, z -+ 2
+    const uint32_t* r = row(z, 0);
+    s[0] = V{r[0]};
+    s[1] = V{r[2]};
+    s[2] = V{row(z, -2)[1]};
+    s[3] = V{row(z, 2)[1]};
+    s[4] = centre(z - 2);
+    s[5] = centre(z + 2);
+  };
+  auto final = [&](const V (&m)[16], const V (&b)[9], const V (&s)[6]) {
+    V w[31];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) w[k] = m[k];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) w[16 + k] = b[k];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w[25 + k] = s[k];
+    net_sphere33_pair_final_raw(w);
+    return w[net_sphere33_pair_final_out[0]];
+  };
+  for (int z = z0 - 2; z <= z0 + 2; ++z) stage(z);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  stage(z0 + 3);
+  stage(z0 + 4);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_group 1;" ::: "memory");
+  __syncthreads();
+  if (xb) {
+    for (int z = z0 - 2; z <= z0 + 2; ++z) fill_plane<SPR>(slot(z), x0, W);
+    __syncthreads();
+  }
+  V bm1[9], b0[9], b1[9], b2[9];  // sorted blocks of planes zo-1 .. zo+2
+  blk(z0 - 1, bm1);
+  blk(z0, b0);
+  blk(z0 + 1, b1);
+  blk(z0 + 2, b2);
+  V s0[6];
+  singles(z0, s0);
+  for (int zo = z0; zo < z1; zo += 2) {
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();  // planes zo+3, zo+4 landed; the reads of zo-3, zo-2 are done
+    if (xb) {
+      fill_plane<SPR>(slot(zo + 3), x0, W);
+      fill_plane<SPR>(slot(zo + 4), x0, W);
+      __syncthreads();
+    }
+    const bool more = zo + 2 < z1;
+    if (more) {  // the next pair's planes zo+5, zo+6 into the buffers of zo-3, zo-2
+      stage(zo + 5);
+      stage(zo + 6);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    V m[16];
+    {
+      V w[18];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) w[k] = b0[k], w[9 + k] = b1[k];
+      net_merge99_r1_16_raw(w);
+      pick(w, net_merge99_r1_16_out, m);
+    }
+    V s1[6];
+    if (zo + 1 < z1) singles(zo + 1, s1);
+    T* o = dst + (int64_t)zo * plane + (int64_t)y * W;
+    if (act) store_pair<T, false>(o, x, W, final(m, bm1, s0));
+    if (more) singles(zo + 2, s0);
+    if (act && zo + 1 < z1) store_pair<T, false>(o + plane, x, W, final(m, b2, s1));
+    if (more) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) bm1[k] = b1[k], b0[k] = b2[k];
+      blk(zo + 3, b1);
+      blk(zo + 4, b2);
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 // median_box_2d 3x3.
 template <class T, bool ODD>
 __device__ __forceinline__ void box9_2d_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int bx,
@@ -603,6 +719,11 @@ __global__ void __launch_bounds__(BX * BY, sphere_pair_min_ctas<T>()) k_median_s
                                                                                      T* __restrict__ dst, int W,
                                                                                      int H, int D, int zchunk) {
   sphere33_pair_tile<T, ODD>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+template <class T>
+__global__ void __launch_bounds__(BX * BY, 2) k_median_sphere33_st(const T* __restrict__ src, T* __restrict__ dst,
+                                                                    int W, int H, int D, int zchunk) {
+  sphere33_staged_tile<T>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 template <class T, bool ODD>
 __global__ void __launch_bounds__(BX * BY, sphere_min_ctas<T>()) k_median_sphere33(const T* __restrict__ src, T* __restrict__ dst, int W,
