@@ -24,7 +24,10 @@
 // three so the ring never moves) and the next plane's pixels in flight.
 // Rows are read as aligned pixel pairs.  Sums convert to float exactly
 // without the I2F unit; the square root is the hardware approximation
-// (relative error far below the 1e-5 bound).
+// (relative error far below the 1e-5 bound).  Unsigned 16-bit images whose
+// rows are whole vectors run the same sums on packed float pairs
+// (k_sobel3d_x2), bit-identical to the integer kernel.
+#include <cstdlib>
 #include <type_traits>
 
 #include "clk_common.cuh"
@@ -439,6 +442,248 @@ __global__ void __launch_bounds__(256, WRAP ? 2 : 3) k_sobel3d_tile(const S* __r
   }
 }
 
+// ---- 16-bit unsigned pixels on packed float pairs.  A pixel value v as a
+// 32-bit word is the float v * 2^-149 (a subnormal), and every partial sum of
+// this kernel is an integer of magnitude below 2^22 times 2^-149, which a
+// float holds exactly; so the sums run as add / fma .rn.f32x2 on the two
+// output columns (x, x+1) of a thread at once, with no conversion from int,
+// and give the integer kernel's sums bit for bit.  The three component sums
+// are then scaled by 2^100 (exact), the 2^32 wrap terms added as K * 2^-17,
+// squared and summed in the integer kernel's order, so every rounding is
+// the same at a scale of 2^-49; the root is scaled back by 2^49.  (Subnormal
+// operands need the non-flushing forms: no .ftz.)
+__device__ __forceinline__ uint64_t u2(uint32_t lo, uint32_t hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(lo), "r"(hi));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2c(float a) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(a));
+  return r;
+}
+__device__ __forceinline__ uint64_t x2add(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t x2sub(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t x2mul(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t x2fma(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+template <bool WRAP>
+__global__ void __launch_bounds__(256, 2) k_sobel3d_x2(const uint16_t* __restrict__ src, float* __restrict__ dst,
+                                                        int W, int H, int D, int zchunk) {
+  using S = uint16_t;
+  constexpr int VE = 8, RA = VE;
+  constexpr int RW = TSX + 2 * RA, RH = TSY + 3;
+  constexpr int SR = RW / VE, NSLOT = RH * SR;
+  static_assert(NSLOT <= 256, "one staging vector per thread");
+  __shared__ __align__(16) S tile[2][RH * RW];
+  const int tid = threadIdx.x, px = tid & 31, py = tid >> 5;
+  const int x0 = blockIdx.x * TSX, y0 = blockIdx.y * TSY;
+  const int x = x0 + 2 * px, y = y0 + 2 * py;
+  const bool act = x < W && y < H;
+  const int z0 = blockIdx.z * zchunk, z1 = min(D, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+
+  uint4 pre = make_uint4(0, 0, 0, 0);
+  auto fetch = [&](int p) {
+    const S* sp = src + (int64_t)clampi(p, D - 1) * plane;
+    if (tid < NSLOT) {
+      const int r = tid / SR, v = tid - r * SR;
+      const S* rowp = sp + (int64_t)clampi(y0 - 1 + r, H - 1) * W;
+      const int gx = x0 - RA + v * VE;
+      pre = (gx >= 0 && gx < W) ? __ldg(reinterpret_cast<const uint4*>(rowp + gx))
+                                : splat16<S>(__ldg(rowp + (gx < 0 ? 0 : W - 1)));
+    }
+  };
+  int pn = z0 - 1;  // the next plane to stage (its pixels are in pre)
+  uint32_t raw[4][3];
+  auto next_plane = [&]() {
+    S* t = tile[(pn - z0 + 1) & 1];
+    if (tid < NSLOT) reinterpret_cast<uint4*>(t)[tid] = pre;
+    if (pn + 1 <= z1 + 1) fetch(pn + 1);
+    ++pn;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const uint32_t* row = reinterpret_cast<const uint32_t*>(t + (2 * py + r) * RW + RA + 2 * px - 2);
+      raw[r][0] = row[0], raw[r][1] = row[1], raw[r][2] = row[2];
+    }
+  };
+
+  const uint64_t two = f2c(2.0f);
+  // per output row oy: A, B, C of the ring planes and the newest plane's E
+  // terms, as (x, x+1) pairs
+  uint64_t A[3][2], B[3][2], C[3][2], ex[2], ey[2], ez[2];
+  uint32_t Zr[3][2] = {}, Ec[2] = {};  // zero-pixel counts, as in k_sobel3d_tile
+  auto terms = [&](uint64_t (&a)[2], uint64_t (&b)[2], uint64_t (&c)[2], uint32_t (&zq)[2]) {
+    uint32_t v[4][4];  // rows y-1 .. y+2, columns x-1 .. x+2
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      v[r][0] = raw[r][0] >> 16;
+      v[r][1] = raw[r][1] & 0xFFFFu;
+      v[r][2] = raw[r][1] >> 16;
+      v[r][3] = raw[r][2] & 0xFFFFu;
+    }
+    if constexpr (WRAP) {
+      // a zero among the 4 x 4 pixels: min over the packed middle words and
+      // the outer columns' pairs (x-1, x+2)
+      uint32_t m = __byte_perm(raw[0][0], raw[0][2], 0x5432);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        m = __vminu2(m, raw[r][1]);
+        if (r) m = __vminu2(m, __byte_perm(raw[r][0], raw[r][2], 0x5432));
+      }
+      zq[0] = zq[1] = Ec[0] = Ec[1] = 0;
+      if ((m & 0xFFFFu) == 0 || (m >> 16) == 0) {
+        uint32_t zr[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) zr[r][c] = v[r][c] == 0 ? 1u : 0u;
+#pragma unroll
+        for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+          for (int ox = 0; ox < 2; ++ox) {
+            const int rm = oy, rc = oy + 1, rp = oy + 2, sh = 16 * ox;
+            const uint32_t zx = zr[rm][ox + 2] + zr[rc][ox + 2] + zr[rp][ox + 2];
+            const uint32_t zy = zr[rp][ox] + zr[rp][ox + 1] + zr[rp][ox + 2];
+            const uint32_t zz = zr[rm][ox] + zr[rm][ox + 1] + zr[rm][ox + 2] + zr[rc][ox] + zr[rc][ox + 1] +
+                                zr[rc][ox + 2] + zy;
+            const uint32_t e_x = zr[rp][ox + 1] + zr[rm][ox + 2] + zr[rc][ox + 2];
+            const uint32_t e_y = zr[rc][ox] + zr[rc][ox + 1] + zr[rc][ox + 2];
+            zq[oy] |= (zx | (zy << 4) | (zz << 8)) << sh;
+            Ec[oy] |= (e_x | (e_y << 4)) << sh;
+          }
+      }
+    }
+    uint64_t p12[4], sx[4], dx[4], p01r[2];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const uint64_t p01 = u2(v[r][0], v[r][1]), p23 = u2(v[r][2], v[r][3]);
+      p12[r] = u2(v[r][1], v[r][2]);
+      sx[r] = x2add(x2fma(p12[r], two, p01), p23);
+      dx[r] = x2sub(p01, p23);
+      if (r >= 2) p01r[r - 2] = p01;
+    }
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy) {
+      const int rm = oy, rc = oy + 1, rp = oy + 2;
+      a[oy] = x2add(x2fma(dx[rc], two, dx[rm]), dx[rp]);
+      b[oy] = x2sub(sx[rm], sx[rp]);
+      c[oy] = x2add(x2fma(sx[rc], two, sx[rm]), sx[rp]);
+      const uint64_t q = x2fma(p01r[oy], two, p12[rp]);
+      ex[oy] = x2sub(x2fma(dx[rm], two, dx[rc]), p12[rp]);
+      ey[oy] = x2sub(q, sx[rc]);
+      ez[oy] = x2add(x2fma(sx[rm], two, sx[rc]), q);
+    }
+  };
+  auto step = [&](int zo, auto i0c, auto i1c, auto i2c) {
+    constexpr int i0 = decltype(i0c)::value, i1 = decltype(i1c)::value, i2 = decltype(i2c)::value;
+    uint64_t a[2], b[2], c[2];
+    uint32_t zq[2];
+    next_plane();  // plane zo + 2
+    terms(a, b, c, zq);
+    const uint64_t up = f2c(0x1p100f);
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy) {
+      const uint64_t sxv = x2add(x2add(x2fma(A[i1][oy], two, A[i0][oy]), A[i2][oy]), ex[oy]);
+      const uint64_t syv = x2add(x2add(x2fma(B[i1][oy], two, B[i0][oy]), B[i2][oy]), ey[oy]);
+      const uint64_t szv = x2add(x2sub(C[i0][oy], C[i2][oy]), ez[oy]);
+      uint64_t fx = x2mul(sxv, up), fy = x2mul(syv, up), fz = x2mul(szv, up);
+      if constexpr (WRAP) {
+        // + K * 2^32 at the scale 2^-49: K = 12, 12, 9 taps minus the zero
+        // pixels among them
+        uint64_t kx = f2c(12.0f * 0x1p-17f), ky = kx, kz = f2c(9.0f * 0x1p-17f);
+        if (Zr[i0][oy] | Zr[i1][oy] | Zr[i2][oy] | Ec[oy]) {
+          const uint32_t sum = Zr[i0][oy] + Zr[i1][oy] + Zr[i2][oy];  // fields <= 9: no carry between them
+          float k[3][2];
+#pragma unroll
+          for (int ox = 0; ox < 2; ++ox) {
+            const int sh = 16 * ox;
+            k[0][ox] = (float)(12 - (int)(((sum >> sh) & 0xFu) + ((Ec[oy] >> sh) & 0xFu))) * 0x1p-17f;
+            k[1][ox] = (float)(12 - (int)(((sum >> (sh + 4)) & 0xFu) + ((Ec[oy] >> (sh + 4)) & 0xFu))) * 0x1p-17f;
+            k[2][ox] = (float)(9 - (int)((Zr[i2][oy] >> (sh + 8)) & 0xFu)) * 0x1p-17f;
+          }
+          kx = u2(__float_as_uint(k[0][0]), __float_as_uint(k[0][1]));
+          ky = u2(__float_as_uint(k[1][0]), __float_as_uint(k[1][1]));
+          kz = u2(__float_as_uint(k[2][0]), __float_as_uint(k[2][1]));
+        }
+        fx = x2add(fx, kx);
+        fy = x2add(fy, ky);
+        fz = x2add(fz, kz);
+      }
+      const uint64_t s = x2fma(fx, fx, x2fma(fy, fy, x2mul(fz, fz)));
+      uint32_t s0, s1;
+      asm("mov.b64 {%0, %1}, %2;" : "=r"(s0), "=r"(s1) : "l"(s));
+      const uint64_t res = x2mul(u2(__float_as_uint(sqrt_approx(__uint_as_float(s0))),
+                                    __float_as_uint(sqrt_approx(__uint_as_float(s1)))),
+                                 f2c(0x1p49f));
+      if (act && y + oy < H)
+        *reinterpret_cast<uint64_t*>(dst + (int64_t)zo * plane + (int64_t)(y + oy) * W + x) = res;
+    }
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy) {
+      Zr[i0][oy] = zq[oy];
+      A[i0][oy] = a[oy], B[i0][oy] = b[oy], C[i0][oy] = c[oy];
+    }
+  };
+
+  fetch(z0 - 1);
+  next_plane();
+  terms(A[0], B[0], C[0], Zr[0]);
+  next_plane();
+  terms(A[1], B[1], C[1], Zr[1]);
+  next_plane();
+  terms(A[2], B[2], C[2], Zr[2]);
+  using I0 = std::integral_constant<int, 0>;
+  using I1 = std::integral_constant<int, 1>;
+  using I2 = std::integral_constant<int, 2>;
+  for (int zo = z0; zo < z1; zo += 3) {
+    step(zo, I0{}, I1{}, I2{});
+    if (zo + 1 < z1) step(zo + 1, I1{}, I2{}, I0{});
+    if (zo + 2 < z1) step(zo + 2, I2{}, I0{}, I1{});
+  }
+}
+
+// CLK_SOBEL_X2=0 in the environment keeps 16-bit pixels on the integer
+// kernel (A/B timing)
+bool x2_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("CLK_SOBEL_X2");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+template <bool WRAP> clk_status launch_sobel_x2(const Image& dst, const Image& src, cudaStream_t st) {
+  const int tx = (src.w + TSX - 1) / TSX, ty = (src.h + TSY - 1) / TSY;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int chunks = 1;
+  while ((int64_t)tx * ty * chunks < 6LL * sms && src.d / (chunks * 2) >= 16) chunks *= 2;
+  const int zchunk = (src.d + chunks - 1) / chunks;
+  k_sobel3d_x2<WRAP><<<dim3(tx, ty, (src.d + zchunk - 1) / zchunk), 256, 0, st>>>(
+      (const uint16_t*)src.ptr, (float*)dst.ptr, src.w, src.h, src.d, zchunk);
+  count_launch();
+  return check_launch("sobel_3d (float pairs)");
+}
+
 template <class S, bool WRAP> clk_status launch_sobel_tile(const Image& dst, const Image& src, cudaStream_t st) {
   const int tx = (src.w + TSX - 1) / TSX, ty = (src.h + TSY - 1) / TSY;
   int dev = 0, sms = 152;
@@ -480,6 +725,7 @@ clk_status fast_sobel(const Image& dst, const Image& src, const Policy& p, cudaS
   if ((uintptr_t)src.ptr % 16 == 0 && src.w % ve == 0) {
     switch (src.dt) {
       case CLK_U16:
+        if (x2_enabled()) return wrap ? launch_sobel_x2<true>(dst, src, st) : launch_sobel_x2<false>(dst, src, st);
         return wrap ? launch_sobel_tile<uint16_t, true>(dst, src, st) : launch_sobel_tile<uint16_t, false>(dst, src, st);
       case CLK_U8:
         return wrap ? launch_sobel_tile<uint8_t, true>(dst, src, st) : launch_sobel_tile<uint8_t, false>(dst, src, st);
