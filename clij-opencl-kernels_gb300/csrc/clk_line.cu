@@ -234,11 +234,33 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
           return OP == MIN ? (b < a ? b : a) : (a < b ? b : a);
         }
       };
+      // Float pixels: fminf / fmaxf (one instruction, NaN never chosen) give
+      // first()'s value wherever that value is not a zero: equal nonzero
+      // floats are the same bits, and a zero can be the extreme only when the
+      // result is one.  So outputs whose centre is NaN take the centre and
+      // zero results (the sign of a zero depends on which one comes first)
+      // rerun the reference's loop over their window.
       auto firstl = [&](const Lane<OP, T>& a, const Lane<OP, T>& b) {
         Lane<OP, T> r;
-        r.a = first(a.a, b.a), r.b = first(a.b, b.b);
+        if constexpr (std::is_same<T, float>::value) {
+          r.a = OP == MIN ? fminf(a.a, b.a) : fmaxf(a.a, b.a);
+          r.b = OP == MIN ? fminf(a.b, b.b) : fmaxf(a.b, b.b);
+        } else {
+          r.a = first(a.a, b.a), r.b = first(a.b, b.b);
+        }
         return r;
       };
+      auto exact = [&](int t, int ln) -> T {  // the reference's loop for output t, lane ln
+        const Lane<OP, T> c = get(base + t + R);
+        T r = ln ? c.b : c.a;
+        for (int k = 0; k <= 2 * R; ++k) {
+          const Lane<OP, T> v = get(base + t + k);
+          const T x = ln ? v.b : v.a;
+          r = (OP == MIN ? x < r : r < x) ? x : r;
+        }
+        return r;
+      };
+      (void)exact;
       Lane<OP, T> suf[M];
       suf[M - 1] = get(base + M - 1);
 #pragma unroll
@@ -251,10 +273,12 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
         const int k = 2 * R + t;
         if (k > M) pre = firstl(pre, get(base + k));
         Lane<OP, T> o = firstl(suf[t], pre);
-        if constexpr (std::is_same<T, float>::value) {  // the centre first, unless it is NaN
+        if constexpr (std::is_same<T, float>::value) {  // a NaN centre is the result; zeros exactly
           const Lane<OP, T> c = get(base + t + R);
-          o.a = c.a != c.a ? c.a : first(c.a, o.a);
-          o.b = c.b != c.b ? c.b : first(c.b, o.b);
+          if (c.a != c.a) o.a = c.a;
+          else if (o.a == 0.f) o.a = exact(t, 0);
+          if (c.b != c.b) o.b = c.b;
+          else if (o.b == 0.f) o.b = exact(t, 1);
         }
         ra[t] = (D)o.a, rb[t] = (D)o.b;
       }
