@@ -103,6 +103,15 @@ template <class T, bool ODD> clk_status launch(Shape sh, const Image& dst, const
         done = true;
       }
     }
+    if constexpr (sizeof(T) == 4) {  // float rows of whole vectors: keys staged in shared memory
+      if (sh == SPHERE33 && staged_enabled() && src.w % 4 == 0 &&
+          ((uintptr_t)src.ptr | (uintptr_t)dst.ptr) % 16 == 0) {
+        const dim3 gf((src.w + BX - 1) / BX, grid.y, grid.z);
+        k_median_sphere33_stf<float><<<gf, block, 0, st>>>((const float*)src.ptr, (float*)dst.ptr, src.w, src.h, src.d,
+                                                    zchunk);
+        done = true;
+      }
+    }
     if (done) {
     } else if (sh == BOX27)
       k_median_box27<T, ODD><<<grid, block, 0, st>>>((const T*)src.ptr, (T*)dst.ptr, src.w, src.h, src.d, zchunk);

@@ -670,6 +670,141 @@ __device__ __forceinline__ void sphere33_staged_tile(const T* __restrict__ src, 
   asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
+// The same z-pair sphere median for float images whose rows are whole
+// 16-byte vectors: one output column per thread (a 32 x 8 tile), each
+// pixel's order-preserving key computed once in shared memory by the thread
+// that copied it (cp.async lands the raw floats; the copying thread waits for
+// its own group, converts its vector in place, and the barrier publishes the
+// keys).  Outside vectors hold the key of the row's edge pixel, read from
+// global memory when the plane is issued.  Rows y0-2 .. y0+BY+1, columns
+// x0-4 .. x0+35, in the same ring of eight planes.
+struct Key1 {
+  uint32_t v;
+};
+__device__ __forceinline__ Key1 vmin(Key1 a, Key1 b) { return Key1{min(a.v, b.v)}; }
+__device__ __forceinline__ Key1 vmax(Key1 a, Key1 b) { return Key1{max(a.v, b.v)}; }
+constexpr int FSW = BX + 8;    // staged floats per row
+constexpr int FSV = FSW / 4;   // 16-byte vectors per row
+static_assert(SPR * FSV <= BX * BY, "one staging vector per thread");
+
+__device__ __forceinline__ void sphere33_staged_f32_tile(const float* __restrict__ src, float* __restrict__ dst,
+                                                         int W, int H, int D, int zchunk, int bx, int by, int bz) {
+  using V = Key1;
+  __shared__ __align__(16) uint32_t buf[8][SPR * FSW];
+  const int tid = threadIdx.x, px = tid % BX, py = tid / BX;
+  const int x0 = bx * BX, y0 = by * BY;
+  const int x = x0 + px, y = y0 + py;
+  const bool act = x < W && y < H;
+  const int z0 = bz * zchunk, z1 = min(D, z0 + zchunk);
+  const int64_t plane = (int64_t)W * H;
+  // this thread's staging vector: row sr, columns x0-4+4sv .. +3
+  const int sr = tid / FSV, sv = tid - sr * FSV, sgx = x0 - 4 + 4 * sv;
+  const bool stager = tid < SPR * FSV, inside = sgx >= 0 && sgx < W;
+  const int64_t srow = (int64_t)clampi(y0 - 2 + sr, H - 1) * W;
+  auto slot = [&](int z) { return buf[(z - z0 + 2) & 7]; };
+  auto stage = [&](int z) {
+    if (!stager) return;
+    const float* p = src + (int64_t)clampi(z, D - 1) * plane + srow;
+    uint32_t* b = slot(z) + sr * FSW + 4 * sv;
+    if (inside) {
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(b)),
+                   "l"(p + sgx)
+                   : "memory");
+    } else {
+      const uint32_t k = fkey(__ldg(p + (sgx < 0 ? 0 : W - 1)));
+      *reinterpret_cast<uint4*>(b) = make_uint4(k, k, k, k);
+    }
+  };
+  auto convert = [&](int z) {  // after this thread's copies landed: floats to keys in place
+    if (!stager || !inside) return;
+    uint4* b = reinterpret_cast<uint4*>(slot(z) + sr * FSW + 4 * sv);
+    const uint4 f = *b;
+    *b = make_uint4(fkey(__uint_as_float(f.x)), fkey(__uint_as_float(f.y)), fkey(__uint_as_float(f.z)),
+                    fkey(__uint_as_float(f.w)));
+  };
+  auto row = [&](int z, int dy) { return slot(z) + (py + 2 + dy) * FSW + px + 4; };  // key of (x, y+dy)
+  auto blk = [&](int z, V (&p)[9]) {
+    V w[9];
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy) {
+      const uint32_t* r = row(z, dy);
+      w[dy + 1] = V{r[-1]};
+      w[dy + 4] = V{r[0]};
+      w[dy + 7] = V{r[1]};
+    }
+    sort9(w, p);
+  };
+  auto centre = [&](int z) { return V{row(z, 0)[0]}; };
+  auto singles = [&](int z, V (&s)[6]) {
+    const uint32_t* r = row(z, 0);
+    s[0] = V{r[-2]};
+    s[1] = V{r[2]};
+    s[2] = V{row(z, -2)[0]};
+    s[3] = V{row(z, 2)[0]};
+    s[4] = centre(z - 2);
+    s[5] = centre(z + 2);
+  };
+  auto final = [&](const V (&m)[16], const V (&b)[9], const V (&s)[6]) {
+    V w[31];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) w[k] = m[k];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) w[16 + k] = b[k];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w[25 + k] = s[k];
+    net_sphere33_pair_final_raw(w);
+    return w[net_sphere33_pair_final_out[0]];
+  };
+  for (int z = z0 - 2; z <= z0 + 2; ++z) stage(z);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  stage(z0 + 3);
+  stage(z0 + 4);
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_group 1;" ::: "memory");
+  for (int z = z0 - 2; z <= z0 + 2; ++z) convert(z);
+  __syncthreads();
+  V bm1[9], b0[9], b1[9], b2[9];  // sorted blocks of planes zo-1 .. zo+2
+  blk(z0 - 1, bm1);
+  blk(z0, b0);
+  blk(z0 + 1, b1);
+  blk(z0 + 2, b2);
+  V s0[6];
+  singles(z0, s0);
+  for (int zo = z0; zo < z1; zo += 2) {
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    convert(zo + 3);
+    convert(zo + 4);
+    __syncthreads();  // planes zo+3, zo+4 hold keys; the reads of zo-3, zo-2 are done
+    const bool more = zo + 2 < z1;
+    if (more) {  // the next pair's planes zo+5, zo+6 into the buffers of zo-3, zo-2
+      stage(zo + 5);
+      stage(zo + 6);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    V m[16];
+    {
+      V w[18];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) w[k] = b0[k], w[9 + k] = b1[k];
+      net_merge99_r1_16_raw(w);
+      pick(w, net_merge99_r1_16_out, m);
+    }
+    V s1[6];
+    if (zo + 1 < z1) singles(zo + 1, s1);
+    float* o = dst + (int64_t)zo * plane + (int64_t)y * W + x;
+    if (act) *o = fval(final(m, bm1, s0).v);
+    if (more) singles(zo + 2, s0);
+    if (act && zo + 1 < z1) o[plane] = fval(final(m, b2, s1).v);
+    if (more) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) bm1[k] = b1[k], b0[k] = b2[k];
+      blk(zo + 3, b1);
+      blk(zo + 4, b2);
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 // median_box_2d 3x3.
 template <class T, bool ODD>
 __device__ __forceinline__ void box9_2d_tile(const T* __restrict__ src, T* __restrict__ dst, int W, int H, int bx,
@@ -724,6 +859,11 @@ template <class T>
 __global__ void __launch_bounds__(BX * BY, 2) k_median_sphere33_st(const T* __restrict__ src, T* __restrict__ dst,
                                                                     int W, int H, int D, int zchunk) {
   sphere33_staged_tile<T>(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+template <class T>  // T = float (a template: this header is included by several translation units)
+__global__ void __launch_bounds__(BX * BY, 2) k_median_sphere33_stf(const T* __restrict__ src, T* __restrict__ dst,
+                                                                     int W, int H, int D, int zchunk) {
+  sphere33_staged_f32_tile(src, dst, W, H, D, zchunk, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 template <class T, bool ODD>
 __global__ void __launch_bounds__(BX * BY, sphere_min_ctas<T>()) k_median_sphere33(const T* __restrict__ src, T* __restrict__ dst, int W,

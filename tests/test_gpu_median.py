@@ -38,7 +38,10 @@ CASES = [("median_box_3d", {"Nx": 3, "Ny": 3, "Nz": 3}), ("median_sphere_3d", {"
 @pytest.mark.parametrize("dt", [np.uint16, np.int16, np.uint8, np.int8, np.float32])
 def test_network_median_3d(clk, oracle, kernel, params, dt):
     rng = np.random.default_rng(23)
-    for shp in ((21, 37, 130), (1, 5, 64), (2, 1, 2), (7, 64, 2), (33, 16, 66), (9, 13, 67), (4, 6, 1), (3, 5, 3)):
+    # widths of whole 16-byte vectors (the staged kernels: 8 pixels of 16 bits, 4 floats) with
+    # partial tiles and both x borders, and widths that take the unstaged kernels
+    for shp in ((21, 37, 130), (1, 5, 64), (2, 1, 2), (7, 64, 2), (33, 16, 66), (9, 13, 67), (4, 6, 1), (3, 5, 3),
+                (21, 37, 132), (5, 9, 36), (11, 40, 96), (6, 19, 8)):
         for lo, hi in ((None, None), (0, 3)):  # full range, and many ties
             a = random_image(rng, shp, dt)
             if lo is not None:
