@@ -114,6 +114,26 @@ clk_status separable_plan(const char* kernel_name, const clk_image* dst, const c
                           const float s[3], const clk_define* defines, size_t ndefines, SepPlan* plan,
                           bool may_allocate = true);
 
+// z-chunks per tile for a kernel whose CTAs each stream one tile through a
+// z-chunk: the count c (1..maxc) that minimises waves(c) x (planes per chunk
+// + halo), waves = ceil(tiles x chunks / slots) and slots = resident CTAs of
+// the whole GPU; chunks are whole multiples of `step` planes.  (A last wave
+// that fills a fraction of the GPU costs as much as a full one.)
+inline int wave_chunks(int64_t tiles, int depth, int halo, int64_t slots, int step = 1, int maxc = 16) {
+  int best = 1;
+  double best_cost = 0;
+  for (int c = 1; c <= maxc; ++c) {
+    int zc = (depth + c - 1) / c;
+    zc = (zc + step - 1) / step * step;
+    const int n = (depth + zc - 1) / zc;  // chunks actually launched
+    if (c > 1 && n < c) break;
+    const double waves = (double)((tiles * n + slots - 1) / slots);
+    const double cost = waves * (zc + halo);
+    if (c == 1 || cost < best_cost * 0.99) best = c, best_cost = cost;
+  }
+  return best;
+}
+
 // ---- generic ("direct") kernels: one thread per output voxel, every
 // pixel-type pair, the reference's own evaluation order (bit-exact).
 clk_status direct_sep_pass(SepOp op, const Image& dst, const Image& src, int dim, const SepTaps& taps, Range r,

@@ -31,6 +31,7 @@
 #include <type_traits>
 
 #include "clk_common.cuh"
+#include "clk_internal.h"
 
 namespace clk {
 
@@ -672,11 +673,18 @@ bool x2_enabled() {
 
 template <bool WRAP> clk_status launch_sobel_x2(const Image& dst, const Image& src, cudaStream_t st) {
   const int tx = (src.w + TSX - 1) / TSX, ty = (src.h + TSY - 1) / TSY;
-  int dev = 0, sms = 152;
+  int dev = 0, sms = 152, per_sm = 2;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int chunks = 1;
-  while ((int64_t)tx * ty * chunks < 6LL * sms && src.d / (chunks * 2) >= 16) chunks *= 2;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sobel3d_x2<WRAP>, 256, 0);
+  // whole waves of resident CTAs; each chunk re-reads 3 halo planes
+  int chunks = wave_chunks((int64_t)tx * ty, src.d, 3, (int64_t)sms * (per_sm > 0 ? per_sm : 1), 1,
+                           src.d / 16 > 1 ? src.d / 16 : 1);
+  static const int forced = [] {  // CLK_SOBEL_CHUNKS=n fixes the z-chunks per tile (A/B timing)
+    const char* e = getenv("CLK_SOBEL_CHUNKS");
+    return e ? atoi(e) : 0;
+  }();
+  if (forced > 0) chunks = forced < src.d ? forced : src.d;
   const int zchunk = (src.d + chunks - 1) / chunks;
   k_sobel3d_x2<WRAP><<<dim3(tx, ty, (src.d + zchunk - 1) / zchunk), 256, 0, st>>>(
       (const uint16_t*)src.ptr, (float*)dst.ptr, src.w, src.h, src.d, zchunk);
