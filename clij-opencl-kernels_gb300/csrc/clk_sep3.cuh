@@ -75,12 +75,16 @@ struct P3 {
 
 __host__ __device__ constexpr int rup(int v, int m) { return (v + m - 1) / m * m; }
 
-// f(integral_constant<int, 0>) ... f(integral_constant<int, N-1>), in order
-template <class F, int... I> __device__ __forceinline__ void static_for_seq(F&& f, std::integer_sequence<int, I...>) {
-  (f(std::integral_constant<int, I>{}), ...);
-}
-template <int N, class F> __device__ __forceinline__ void static_for(F&& f) {
-  static_for_seq(f, std::make_integer_sequence<int, N>{});
+// f(integral_constant<int, s>) for a runtime s in [LO, HI), by binary search:
+// ceil(log2(HI - LO)) compares instead of one per value
+template <int LO, int HI, class F> __device__ __forceinline__ void dispatch(int s, F&& f) {
+  if constexpr (HI - LO == 1) {
+    f(std::integral_constant<int, LO>{});
+  } else {
+    constexpr int MID = (LO + HI) / 2;
+    if (s < MID) dispatch<LO, MID>(s, f);
+    else dispatch<MID, HI>(s, f);
+  }
 }
 
 template <int OP, int R, int CZ, class C> struct Geo {
@@ -556,9 +560,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
       if (yvalid) {
         ypass(XS0 + nxt * G::XS_BYTES);
         // one copy of the ring step per slot, so that every slot is a fixed register
-        static_for<NZ>([&](auto kc) {
-          if (slot == decltype(kc)::value) zstep(it - 1, kc);
-        });
+        dispatch<0, NZ>(slot, [&](auto kc) { zstep(it - 1, kc); });
       }
       slot = slot + 1 == NZ ? 0 : slot + 1;
     }
