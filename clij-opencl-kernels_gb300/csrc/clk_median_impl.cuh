@@ -396,7 +396,12 @@ __device__ __forceinline__ void box27_staged_tile(const T* __restrict__ src, T* 
   stage_plane_async<SMR, 1>(pl(z0 + 2), x0, y0, W, H, buf[3]);
   asm volatile("cp.async.commit_group;" ::: "memory");
   int slot = 2;  // buffers of planes zo+1, zo+2
-  for (int zo = z0; zo < z1; zo += 2) {
+  // one z pair: the blocks of planes zo-1, zo (pm1, p0; row y: a, row y+1:
+  // b) are read, those of zo+1, zo+2 written to p1, p2.  Two calls per loop
+  // trip with the sets swapped, so the blocks never move between registers.
+  typedef V Blk[9];
+  auto pair = [&](int zo, const Blk& am1_, const Blk& bm1_, const Blk& a0_, const Blk& b0_, Blk& a1_, Blk& b1_,
+                  Blk& a2_, Blk& b2_) {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();  // planes zo+1, zo+2 landed; the other pair's last reads are done
     if (xb) {
@@ -412,25 +417,28 @@ __device__ __forceinline__ void box27_staged_tile(const T* __restrict__ src, T* 
     asm volatile("cp.async.commit_group;" ::: "memory");
     rows4_smem(buf[slot], px, py, q1);
     rows4_smem(buf[slot + 1], px, py, q2);
-    V a1[9], b1[9], a2[9], b2[9];
-    blocks_ypair(q1, a1, b1);
-    blocks_ypair(q2, a2, b2);
+    blocks_ypair(q1, a1_, b1_);
+    blocks_ypair(q2, a2_, b2_);
     T* o0 = dst + (int64_t)zo * plane + (int64_t)y * W;
     if (act) {
       V m[10];
-      merge_mid(a0, a1, m);
-      store_pair<T, false>(o0, x, W, final27(m, am1));
-      if (zo + 1 < z1) store_pair<T, false>(o0 + plane, x, W, final27(m, a2));
+      merge_mid(a0_, a1_, m);
+      store_pair<T, false>(o0, x, W, final27(m, am1_));
+      if (zo + 1 < z1) store_pair<T, false>(o0 + plane, x, W, final27(m, a2_));
     }
     if (act && two) {
       V m[10];
-      merge_mid(b0, b1, m);
-      store_pair<T, false>(o0 + W, x, W, final27(m, bm1));
-      if (zo + 1 < z1) store_pair<T, false>(o0 + plane + W, x, W, final27(m, b2));
+      merge_mid(b0_, b1_, m);
+      store_pair<T, false>(o0 + W, x, W, final27(m, bm1_));
+      if (zo + 1 < z1) store_pair<T, false>(o0 + plane + W, x, W, final27(m, b2_));
     }
-#pragma unroll
-    for (int k = 0; k < 9; ++k) am1[k] = a1[k], bm1[k] = b1[k], a0[k] = a2[k], b0[k] = b2[k];
     slot = nslot;
+  };
+  V a1[9], b1[9], a2[9], b2[9];
+  for (int zo = z0; zo < z1; zo += 4) {
+    pair(zo, am1, bm1, a0, b0, a1, b1, a2, b2);
+    if (zo + 2 >= z1) break;
+    pair(zo + 2, a1, b1, a2, b2, am1, bm1, a0, b0);
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
@@ -632,7 +640,11 @@ __device__ __forceinline__ void sphere33_staged_tile(const T* __restrict__ src, 
   blk(z0 + 2, b2);
   V s0[6];
   singles(z0, s0);
-  for (int zo = z0; zo < z1; zo += 2) {
+  // one z pair from the blocks of planes zo-1 .. zo+2 (pm1, p0, p1, p2); the
+  // next pair's zo+3, zo+4 replace pm1, p0.  Two calls per loop trip with
+  // the sets swapped, so the blocks never move between registers.
+  typedef V Blk[9];
+  auto pair = [&](int zo, Blk& pm1, Blk& p0, const Blk& p1, const Blk& p2) {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();  // planes zo+3, zo+4 landed; the reads of zo-3, zo-2 are done
     if (xb) {
@@ -650,22 +662,25 @@ __device__ __forceinline__ void sphere33_staged_tile(const T* __restrict__ src, 
     {
       V w[18];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) w[k] = b0[k], w[9 + k] = b1[k];
+      for (int k = 0; k < 9; ++k) w[k] = p0[k], w[9 + k] = p1[k];
       net_merge99_r1_16_raw(w);
       pick(w, net_merge99_r1_16_out, m);
     }
     V s1[6];
     if (zo + 1 < z1) singles(zo + 1, s1);
     T* o = dst + (int64_t)zo * plane + (int64_t)y * W;
-    if (act) store_pair<T, false>(o, x, W, final(m, bm1, s0));
+    if (act) store_pair<T, false>(o, x, W, final(m, pm1, s0));
     if (more) singles(zo + 2, s0);
-    if (act && zo + 1 < z1) store_pair<T, false>(o + plane, x, W, final(m, b2, s1));
+    if (act && zo + 1 < z1) store_pair<T, false>(o + plane, x, W, final(m, p2, s1));
     if (more) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) bm1[k] = b1[k], b0[k] = b2[k];
-      blk(zo + 3, b1);
-      blk(zo + 4, b2);
+      blk(zo + 3, pm1);
+      blk(zo + 4, p0);
     }
+  };
+  for (int zo = z0; zo < z1; zo += 4) {
+    pair(zo, bm1, b0, b1, b2);
+    if (zo + 2 >= z1) break;
+    pair(zo + 2, b1, b2, bm1, b0);
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
@@ -770,7 +785,8 @@ __device__ __forceinline__ void sphere33_staged_f32_tile(const float* __restrict
   blk(z0 + 2, b2);
   V s0[6];
   singles(z0, s0);
-  for (int zo = z0; zo < z1; zo += 2) {
+  typedef V Blk[9];  // z pairs with the block sets swapped, as in the 16-bit kernel
+  auto pair = [&](int zo, Blk& pm1, Blk& p0, const Blk& p1, const Blk& p2) {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     convert(zo + 3);
     convert(zo + 4);
@@ -785,22 +801,25 @@ __device__ __forceinline__ void sphere33_staged_f32_tile(const float* __restrict
     {
       V w[18];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) w[k] = b0[k], w[9 + k] = b1[k];
+      for (int k = 0; k < 9; ++k) w[k] = p0[k], w[9 + k] = p1[k];
       net_merge99_r1_16_raw(w);
       pick(w, net_merge99_r1_16_out, m);
     }
     V s1[6];
     if (zo + 1 < z1) singles(zo + 1, s1);
     float* o = dst + (int64_t)zo * plane + (int64_t)y * W + x;
-    if (act) *o = fval(final(m, bm1, s0).v);
+    if (act) *o = fval(final(m, pm1, s0).v);
     if (more) singles(zo + 2, s0);
-    if (act && zo + 1 < z1) o[plane] = fval(final(m, b2, s1).v);
+    if (act && zo + 1 < z1) o[plane] = fval(final(m, p2, s1).v);
     if (more) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) bm1[k] = b1[k], b0[k] = b2[k];
-      blk(zo + 3, b1);
-      blk(zo + 4, b2);
+      blk(zo + 3, pm1);
+      blk(zo + 4, p0);
     }
+  };
+  for (int zo = z0; zo < z1; zo += 4) {
+    pair(zo, bm1, b0, b1, b2);
+    if (zo + 2 >= z1) break;
+    pair(zo + 2, b1, b2, bm1, b0);
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
