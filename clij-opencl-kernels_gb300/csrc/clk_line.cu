@@ -7,7 +7,8 @@
 //
 // A CTA owns a tile of 64 lines along the axis x 64 columns across it (two
 // columns per thread, the two lanes of every operation), stages the tile and
-// its 2R-line halo in shared memory, and each thread computes 8 consecutive
+// its 2R-line halo in shared memory (float pixels by cp.async, all of a
+// thread's copies in flight at once), and each thread computes 8 consecutive
 // outputs with a register window that slides one staged line per tap: every
 // tap costs one shared-memory read per 8 outputs, whatever the radius.
 //
@@ -129,7 +130,29 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
   // Loads are batched U deep so that each thread has U in flight.
   constexpr int U = 8;
   const int NP = NLS | 1;
-  if constexpr (AXIS == 0) {
+  if constexpr (std::is_same<S, T>::value) {
+    // float pixels are staged as they are: 4-byte cp.async copies, every one
+    // of the thread's copies in flight at once and no registers held
+    auto cp4 = [](T* d, const S* g) {
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(d)), "l"(g)
+                   : "memory");
+    };
+    if constexpr (AXIS == 0) {
+      for (int l = lane; l < NLS; l += 32) {
+        const int ll = clampi(l0 - R + l, L - 1);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int c = warp + 8 * u;
+          cp4(sm + ((c & 31) * NP + l) * 2 + (c >> 5), src + at(ll, min(c0 + c, C - 1)));
+        }
+      }
+    } else {
+      const int total = NLS * TC;
+      for (int i = tid; i < total; i += NT)
+        cp4(sm + i, src + at(clampi(l0 - R + (i >> 6), L - 1), min(c0 + (i & 63), C - 1)));
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+  } else if constexpr (AXIS == 0) {
     // warp w stages columns (rows of the image) w + 8u, u = 0..7
     for (int l = lane; l < NLS; l += 32) {
       const int ll = clampi(l0 - R + l, L - 1);
