@@ -30,8 +30,9 @@ namespace line {
 namespace {
 
 constexpr int NT = 256;
-constexpr int M = 8;     // outputs per thread along the axis
-constexpr int TL = 64;   // outputs per tile along the axis (8 groups of M)
+// M: outputs per thread along the axis (a template argument: 8, or 16 for
+// the Gaussian along long lines); a tile holds 8 M outputs along the axis,
+// one group of M per warp
 constexpr int TC = 64;   // columns per tile across the axis (32 lane pairs)
 constexpr int kMaxR = 127;
 
@@ -90,12 +91,13 @@ template <class T> struct Lane<GAUSS, T> {
 // AXIS 0: lines along x; the tile's columns are 64 rows (y), lanes = rows
 //   r and r + 32.  AXIS 1 / 2: lines along y / z; columns are 64 x
 //   positions, lanes = x and x + 1.
-template <class S, class D, int OP, int AXIS>
+template <class S, class D, int OP, int AXIS, int M>
 __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __restrict__ dst, int W, int H, int Dz,
                                             const __grid_constant__ Params p) {
   using T = typename Val<S>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
+  constexpr int TL = 8 * M;
   const int R = p.R;
   const int KP = (2 * R + 1 + M - 1) / M * M;  // taps rounded up to whole chunks
   const int NLS = TL + KP;                     // staged lines
@@ -366,8 +368,9 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
   store_out(ra, rb);
 }
 
-template <class S, class D, int OP>
+template <class S, class D, int OP, int M>
 clk_status launch(const Image& dst, const Image& src, int axis, const Params& p, cudaStream_t st) {
+  constexpr int TL = 8 * M;
   const int KP = (2 * p.R + 1 + M - 1) / M * M, NLS = TL + KP;
   const size_t smem = axis == 0 ? (size_t)TC * (NLS | 1) * 4 : (size_t)NLS * TC * 4;
   const int W = src.w, H = src.h, Dz = src.d;
@@ -386,9 +389,21 @@ clk_status launch(const Image& dst, const Image& src, int axis, const Params& p,
     count_launch();
     return check_launch("separable (line pass)");
   };
-  if (axis == 0) return go(k_line<S, D, OP, 0>);
-  if (axis == 1) return go(k_line<S, D, OP, 1>);
-  return go(k_line<S, D, OP, 2>);
+  if (axis == 0) return go(k_line<S, D, OP, 0, M>);
+  if (axis == 1) return go(k_line<S, D, OP, 1, M>);
+  return go(k_line<S, D, OP, 2, M>);
+}
+// The Gaussian along lines of at least 1024 voxels takes 16 outputs per
+// thread (half the window reads and tap loads per FMA, half the halo per
+// tile); other operations, and short lines (whose last tile would be mostly
+// empty), take 8
+template <class S, class D, int OP>
+clk_status launch(const Image& dst, const Image& src, int axis, const Params& p, cudaStream_t st) {
+  if constexpr (OP == GAUSS) {
+    const int L = axis == 0 ? src.w : axis == 1 ? src.h : src.d;
+    if (L >= 1024) return launch<S, D, OP, 16>(dst, src, axis, p, st);
+  }
+  return launch<S, D, OP, 8>(dst, src, axis, p, st);
 }
 
 template <int OP> clk_status by_type(const Image& dst, const Image& src, int axis, const Params& p, cudaStream_t st) {

@@ -82,6 +82,20 @@ def test_gaussian_large_sigma(clk, oracle, dt):
             assert (err <= REL_TOL * np.maximum(np.abs(val), scale)).all(), (shp, np.dtype(dt), s)
 
 
+def test_gaussian_long_lines(clk, oracle):
+    # lines of 1024 voxels or more take 16 outputs per thread (tiles of 128
+    # lines): partial last tiles along each axis in turn
+    rng = np.random.default_rng(75)
+    for shp in ((2, 9, 1100), (2, 1030, 12), (1030, 3, 8)):
+        a = random_image(rng, shp, np.float32)
+        for s in ((10.0, 10.0, 5.0), (5.0, 5.0, 5.0)):
+            N = tuple(2 * int(np.ceil(3 * v)) + 1 for v in s)
+            val, scale = oracle.fp64("gaussian_blur_separable_3d", a, N, s)
+            got = run(clk, "gaussian_blur_separable_3d", a, np.float32, N, s)
+            err = np.abs(got.astype(np.float64) - val)
+            assert (err <= REL_TOL * np.maximum(np.abs(val), scale)).all(), (shp, s)
+
+
 def test_2d_large_radii(clk, oracle):
     rng = np.random.default_rng(74)
     a = random_image(rng, (50, 300), np.uint16)
