@@ -319,7 +319,10 @@ __global__ void __launch_bounds__(NT) k_line(const S* __restrict__ src, D* __res
     else acc[j].v = 0ull;
     win[j] = get(base + j);
   }
-  for (int kk = 0; kk < KP; kk += M) {
+  // a group whose outputs all lie beyond the line (the last tile of a line
+  // that is not a whole number of tiles) skips the taps
+  const int kend = l0 + base < L ? KP : 0;
+  for (int kk = 0; kk < kend; kk += M) {
 #pragma unroll
     for (int t = 0; t < M; ++t) {
       const int k = kk + t;
@@ -393,15 +396,14 @@ clk_status launch(const Image& dst, const Image& src, int axis, const Params& p,
   if (axis == 1) return go(k_line<S, D, OP, 1, M>);
   return go(k_line<S, D, OP, 2, M>);
 }
-// The Gaussian along lines of at least 1024 voxels takes 16 outputs per
+// The Gaussian along lines of at least 256 voxels takes 16 outputs per
 // thread (half the window reads and tap loads per FMA, half the halo per
-// tile); other operations, and short lines (whose last tile would be mostly
-// empty), take 8
+// tile); other operations, and short lines, take 8
 template <class S, class D, int OP>
 clk_status launch(const Image& dst, const Image& src, int axis, const Params& p, cudaStream_t st) {
   if constexpr (OP == GAUSS) {
     const int L = axis == 0 ? src.w : axis == 1 ? src.h : src.d;
-    if (L >= 1024) return launch<S, D, OP, 16>(dst, src, axis, p, st);
+    if (L >= 256) return launch<S, D, OP, 16>(dst, src, axis, p, st);
   }
   return launch<S, D, OP, 8>(dst, src, axis, p, st);
 }

@@ -83,10 +83,11 @@ def test_gaussian_large_sigma(clk, oracle, dt):
 
 
 def test_gaussian_long_lines(clk, oracle):
-    # lines of 1024 voxels or more take 16 outputs per thread (tiles of 128
-    # lines): partial last tiles along each axis in turn
+    # lines of 256 voxels or more take 16 outputs per thread (tiles of 128
+    # lines): partial last tiles along each axis in turn, one with a single
+    # live group
     rng = np.random.default_rng(75)
-    for shp in ((2, 9, 1100), (2, 1030, 12), (1030, 3, 8)):
+    for shp in ((2, 9, 1100), (2, 1030, 12), (1030, 3, 8), (400, 2, 8), (2, 272, 6)):
         a = random_image(rng, shp, np.float32)
         for s in ((10.0, 10.0, 5.0), (5.0, 5.0, 5.0)):
             N = tuple(2 * int(np.ceil(3 * v)) + 1 for v in s)
