@@ -69,6 +69,23 @@ def test_float_minmax_large_radii_with_nan(clk, oracle, kernel):
                 assert got.tobytes() == want.tobytes(), (kernel, shp, N)
 
 
+@pytest.mark.parametrize("kernel", ["minimum_separable_3d", "maximum_separable_3d"])
+def test_float_minmax_long_lines(clk, oracle, kernel):
+    # float min/max along lines of 1024 voxels or more take 16 outputs per
+    # thread: partial last tiles along x and y, dense NaNs and signed zeros
+    rng = np.random.default_rng(76)
+    for shp in ((2, 5, 1100), (2, 1030, 6)):
+        a = random_image(rng, shp, np.float32)
+        a[rng.random(shp) < 0.05] = np.nan
+        a[rng.random(shp) < 0.1] = 0.0
+        a[rng.random(shp) < 0.1] = -0.0
+        for r in ((15, 15, 1), (8, 9, 0), (40, 12, 1)):
+            N = tuple(2 * v + 1 for v in r)
+            want = oracle.separable(kernel, a, np.float32, N, tuple(float(v) for v in r))
+            got = run(clk, kernel, a, np.float32, N, tuple(float(v) for v in r))
+            assert got.tobytes() == want.tobytes(), (kernel, shp, N)
+
+
 @pytest.mark.parametrize("dt", [np.uint16, np.int8, np.float32])
 def test_gaussian_large_sigma(clk, oracle, dt):
     rng = np.random.default_rng(73)
