@@ -485,7 +485,7 @@ __device__ __forceinline__ uint64_t x2fma(uint64_t a, uint64_t b, uint64_t c) {
 }
 
 template <bool WRAP>
-__global__ void __launch_bounds__(256, 2) k_sobel3d_x2(const uint16_t* __restrict__ src, float* __restrict__ dst,
+__global__ void __launch_bounds__(256, 3) k_sobel3d_x2(const uint16_t* __restrict__ src, float* __restrict__ dst,
                                                         int W, int H, int D, int zchunk) {
   using S = uint16_t;
   constexpr int VE = 8, RA = VE;
