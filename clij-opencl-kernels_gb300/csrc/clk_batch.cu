@@ -53,12 +53,34 @@ const void* batch_sep2_kernel(int op, int R, int dt) {
   return nullptr;
 }
 
-const void* batch_median_kernel(int dt) {
+namespace {
+template <class T> const void* median_kernel_t(int algo) {
+  switch (algo) {
+    case A_MED27: return (const void*)k_batch_median<T, A_MED27>;
+    case A_MED9: return (const void*)k_batch_median<T, A_MED9>;
+    case A_MED33: return (const void*)k_batch_median<T, A_MED33>;
+  }
+  if constexpr (sizeof(T) <= 2) {
+    if (algo == A_MED27Y) return (const void*)k_batch_median<T, A_MED27Y>;
+    if (algo == A_MED33P) return (const void*)k_batch_median<T, A_MED33P>;
+  }
+  if constexpr (sizeof(T) == 2) {
+    if (algo == A_MED27S) return (const void*)k_batch_median<T, A_MED27S>;
+    if (algo == A_MED33S) return (const void*)k_batch_median<T, A_MED33S>;
+  }
+  if constexpr (sizeof(T) == 4) {
+    if (algo == A_MED33F) return (const void*)k_batch_median<T, A_MED33F>;
+  }
+  return nullptr;
+}
+}  // namespace
+
+const void* batch_median_kernel(int dt, int algo) {
   switch (dt) {
-    case CLK_U8: return (const void*)k_batch_median<uint8_t>;
-    case CLK_U16: return (const void*)k_batch_median<uint16_t>;
-    case CLK_I16: return (const void*)k_batch_median<int16_t>;
-    case CLK_F32: return (const void*)k_batch_median<float>;
+    case CLK_U8: return median_kernel_t<uint8_t>(algo);
+    case CLK_U16: return median_kernel_t<uint16_t>(algo);
+    case CLK_I16: return median_kernel_t<int16_t>(algo);
+    case CLK_F32: return median_kernel_t<float>(algo);
   }
   return nullptr;
 }
@@ -388,9 +410,16 @@ ImgStep plan_median(clk_batch* b, int s, int i, MedDesc* d) {
   if (in.ndim == 3 && sphere && m.ex == 2 && m.ey == 2 && m.ez == 2 && m.n == 33) algo = A_MED33;
   if (in.ndim == 2 && m.ex == 1 && m.ey == 1 && m.n == 9) algo = A_MED9;
   if (!algo) return h;
+  // even widths take the bodies the plain launcher takes (clk_median.cu)
+  const int sz = dtype_size(in.dt);
+  const bool even = (in.w & 1) == 0, a16 = (((uintptr_t)in.ptr | (uintptr_t)out.ptr) % 16) == 0;
+  if (even && algo == A_MED27 && sz <= 2) algo = sz == 2 && in.w % 8 == 0 && a16 ? A_MED27S : A_MED27Y;
+  if (even && algo == A_MED33 && sz <= 2) algo = sz == 2 && in.w % 8 == 0 && a16 ? A_MED33S : A_MED33P;
+  if (even && algo == A_MED33 && in.dt == CLK_F32 && in.w % 4 == 0 && a16) algo = A_MED33F;
   *d = MedDesc{in.ptr, out.ptr, in.w, in.h, in.d, 0, in.dt, algo};
   h.algo = algo;
-  h.tx = 2 * med::BX, h.ty = med::BY;
+  h.tx = algo == A_MED33F ? med::BX : 2 * med::BX;
+  h.ty = algo == A_MED27Y || algo == A_MED27S ? med::BYP : med::BY;
   return h;
 }
 
@@ -401,7 +430,7 @@ void build_items(clk_batch* b, int s, Group& g, int zc) {
     const clk::Image& im = b->src[i];
     const int tx = (im.w + h.tx - 1) / h.tx, ty = (im.h + h.ty - 1) / h.ty;
     int z = std::max(1, std::min(zc, im.d));
-    if (h.algo == A_MED27) z += z & 1;  // the box median pairs outputs along z
+    if (med_z_pairs(h.algo)) z += z & 1;  // these medians pair outputs along z
     const int tz = h.algo == A_MED9 ? 1 : (im.d + z - 1) / z;
     for (int bz = 0; bz < tz; ++bz)
       for (int by = 0; by < ty; ++by)
@@ -761,16 +790,16 @@ clk_status clk_batch_create(const clk_op* ops, int32_t nops, const clk_image* sr
       for (int i = 0; i < nimages; ++i) {
         b->how[s][i] = plan_median(b, s, i, &hd[i]);
         if (!b->how[s][i].algo) continue;
-        const int dt = b->src[i].dt;
-        if (!gi.count(dt)) {
+        const int dt = b->src[i].dt, key = dt * 16 + b->how[s][i].algo;  // one group per (type, body)
+        if (!gi.count(key)) {
           Group g;
-          g.kernel = batch_median_kernel(dt);
+          g.kernel = batch_median_kernel(dt, b->how[s][i].algo);
           g.median = true;
           g.dt = dt;
-          gi[dt] = (int)b->groups[s].size();
+          gi[key] = (int)b->groups[s].size();
           b->groups[s].push_back(g);
         }
-        b->groups[s][gi[dt]].imgs.push_back(i);
+        b->groups[s][gi[key]].imgs.push_back(i);
       }
       if (cudaMalloc(&b->d_med[s], nimages * sizeof(MedDesc)) != cudaSuccess ||
           cudaMemcpy(b->d_med[s], hd.data(), nimages * sizeof(MedDesc), cudaMemcpyHostToDevice) != cudaSuccess) {

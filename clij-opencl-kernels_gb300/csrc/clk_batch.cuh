@@ -1,6 +1,8 @@
 // clk_batch.cuh - the batch engine's device-side descriptors and the
 // persistent kernels that walk a tile work list over many images.
 #pragma once
+#include <type_traits>
+
 #include "clk_fused_impl.cuh"
 #include "clk_median_impl.cuh"
 #include "clk_sep2_impl.cuh"
@@ -16,8 +18,16 @@ enum Algo : int {
   A_FUSED_FAST = 3,   // generic fused kernel, FMA (float Gaussian)
   A_MED27 = 4,        // median networks (clk_median_impl.cuh)
   A_MED9 = 5,
-  A_MED33 = 6
+  A_MED33 = 6,
+  // even widths, as the plain launcher chooses them:
+  A_MED27Y = 7,   // box median with row pairs (8/16-bit pixels)
+  A_MED27S = 8,   // the same with staged plane tiles (16-bit rows of whole vectors, aligned)
+  A_MED33P = 9,   // sphere median in z pairs (8/16-bit pixels)
+  A_MED33S = 10,  // the same with staged plane tiles (16-bit rows of whole vectors, aligned)
+  A_MED33F = 11   // float sphere median, staged keys (rows of whole vectors, aligned)
 };
+// the median bodies that take their outputs in z pairs (even z-chunks)
+constexpr bool med_z_pairs(int algo) { return algo == A_MED27 || algo >= A_MED27Y; }
 
 struct WorkItem {
   int img;
@@ -99,26 +109,46 @@ __global__ void __launch_bounds__(256) k_batch_sep(const WorkItem* __restrict__ 
   }
 }
 
-template <class T> __device__ __forceinline__ void med_item_t(const MedDesc& d, const WorkItem& it) {
+// One work item of a median step; ALGO picks the body at compile time, so
+// that each kernel carries one network (and that network's registers).
+template <class T, int ALGO> __device__ __forceinline__ void med_item_t(const MedDesc& d, const WorkItem& it) {
   const T* s = static_cast<const T*>(d.src);
   T* o = static_cast<T*>(d.dst);
-  if (d.W & 1) {
-    if (d.algo == A_MED27) med::box27_tile<T, true>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
-    else if (d.algo == A_MED33) med::sphere33_tile<T, true>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
-    else med::box9_2d_tile<T, true>(s, o, d.W, d.H, it.bx, it.by);
+  if constexpr (ALGO == A_MED27 || ALGO == A_MED33 || ALGO == A_MED9) {
+    if (d.W & 1) {
+      if constexpr (ALGO == A_MED27) med::box27_tile<T, true>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+      else if constexpr (ALGO == A_MED33) med::sphere33_tile<T, true>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+      else med::box9_2d_tile<T, true>(s, o, d.W, d.H, it.bx, it.by);
+    } else {
+      if constexpr (ALGO == A_MED27) med::box27_tile<T, false>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+      else if constexpr (ALGO == A_MED33)
+        med::sphere33_tile<T, false>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+      else med::box9_2d_tile<T, false>(s, o, d.W, d.H, it.bx, it.by);
+    }
+  } else if constexpr (ALGO == A_MED27Y) {
+    med::box27_ypair_tile<T, false>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+  } else if constexpr (ALGO == A_MED33P) {
+    med::sphere33_pair_tile<T, false>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+  } else if constexpr (ALGO == A_MED27S) {
+    med::box27_staged_tile<T>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
+  } else if constexpr (ALGO == A_MED33S) {
+    med::sphere33_staged_tile<T>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
   } else {
-    if (d.algo == A_MED27) med::box27_tile<T, false>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
-    else if (d.algo == A_MED33) med::sphere33_tile<T, false>(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
-    else med::box9_2d_tile<T, false>(s, o, d.W, d.H, it.bx, it.by);
+    med::sphere33_staged_f32_tile(s, o, d.W, d.H, d.D, d.zchunk, it.bx, it.by, it.bz);
   }
 }
 
-template <class T>
-__global__ void __launch_bounds__(256) k_batch_median(const WorkItem* __restrict__ items, int n,
-                                                      const MedDesc* __restrict__ descs) {
+// the CTAs per SM each body's registers allow (as the plain kernels launch them)
+template <int ALGO> constexpr int med_min_ctas() { return ALGO >= A_MED27Y ? 2 : 1; }
+
+template <class T, int ALGO>
+__global__ void __launch_bounds__(256, med_min_ctas<ALGO>()) k_batch_median(const WorkItem* __restrict__ items,
+                                                                             int n, const MedDesc* __restrict__ descs) {
   for (int i = blockIdx.x; i < n; i += gridDim.x) {
     const WorkItem it = items[i];
-    med_item_t<T>(descs[it.img], it);
+    med_item_t<T, ALGO>(descs[it.img], it);
+    if constexpr (ALGO == A_MED27S || ALGO == A_MED33S || ALGO == A_MED33F)
+      __syncthreads();  // the staged bodies reuse their shared-memory planes for the next item
   }
 }
 
@@ -129,7 +159,7 @@ template <int OP> const void* batch_sep_kernel_op(int R, int dt);  // one file p
 // the register-window kernel for (op, R >= 1, pixel type); nullptr if none
 const void* batch_sep2_kernel(int op, int R, int dt);
 template <int OP> const void* batch_sep2_kernel_op(int R, int dt);
-const void* batch_median_kernel(int dt);
+const void* batch_median_kernel(int dt, int algo);  // nullptr if not instantiated
 constexpr int kBatchRadii[] = {2, 3, 4, 5, 6};  // instantiated XY radii besides 0
 
 }  // namespace batch

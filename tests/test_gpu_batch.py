@@ -102,7 +102,7 @@ def test_batched_tophat_matches_oracle_on_integer_images(clk, oracle, tmp_path, 
         assert np.array_equal(got[k], cur), (k, a.shape, a.dtype)
 
 
-def test_one_launch_per_step_and_type(clk, tmp_path, monkeypatch):
+def test_one_launch_per_step_type_and_body(clk, tmp_path, monkeypatch):
     import torch
     monkeypatch.setenv("CLK_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
     rng = np.random.default_rng(53)
@@ -114,7 +114,10 @@ def test_one_launch_per_step_and_type(clk, tmp_path, monkeypatch):
     srcs = [torch.from_numpy(a).cuda() for a in imgs]
     dsts = [torch.empty_like(s) for s in srcs]
     b = clk.Batch(CHAIN_TOPHAT(clk), srcs, dsts)
-    assert b.launches <= 4 * 3, b.launches  # steps x pixel types, not steps x images
+    # steps x pixel types, not steps x images; the median step runs one launch
+    # per pixel type and network body (16-bit rows of whole vectors take the
+    # staged tiles, other even widths the row pairs)
+    assert b.launches <= 4 * 3 + 3, b.launches
     b.close()
 
 
