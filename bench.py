@@ -67,6 +67,21 @@ NCU_DRAM_BYTES_PER_VOXEL = {
 # The selection networks are bound by the min/max (ALU) pipe, not by DRAM:
 # its busy fraction from the one-kernel capture of the same kernel.
 NCU_ALU_PIPE_BUSY = {"median_sphere r2": 0.877}
+# Packed 16-bit min/max instructions per voxel of the selection networks
+# (box: 336 per thread and z pair of two rows, 8 voxels; sphere: 334 per
+# thread and z pair of one row, 4 voxels).  Each SM sub-partition issues one
+# such warp instruction every two cycles, which sets the networks' floor.
+NETWORK_MINMAX_PER_VOXEL = {"median_box r1": 42.0, "median_sphere r2": 83.5}
+
+
+def alu_roofline(name, voxels, ms, sms, mhz):
+    """The min/max-pipe floor of a network median and the measured fraction of it."""
+    mm = NETWORK_MINMAX_PER_VOXEL.get(name)
+    if mm is None or not ms or not sms or not mhz:
+        return {}
+    floor_ms = voxels * mm / 32 / (sms * 4 * 0.5 * mhz * 1e6) * 1e3
+    return {"minmax_per_voxel": mm, "alu_floor_ms": round(floor_ms, 4), "alu_frac": round(floor_ms / ms, 4),
+            "alu_floor_basis": f"{sms} SMs x 4 sub-partitions x 1 warp min/max per 2 cycles at {mhz:.0f} MHz"}
 
 
 NOMINAL_HBM_GBS = 7900.0  # GB300 HBM3e, nominal (the measured copy peak is the roofline)
@@ -942,6 +957,13 @@ def main():
         per[name] = {"ms": round(ms, 4), "ms_median": round(statistics.median(runs), 4),
                      "ms_best": round(min(runs), 4), "gvox_s": round(V / (ms * 1e-3) / 1e9, 2),
                      "hbm_frac": round(gbs / peak, 4), "bytes_per_voxel": bpv}
+    try:  # the networks' ALU floor at the sampled SM clock (the maximum clock if none was sampled)
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        mhz = (clocks.result or {}).get("sm_mhz") or 2070.0
+        for name in per:
+            per[name].update(alu_roofline(name, V, per[name]["ms"], sms, mhz))
+    except Exception:  # informational only
+        pass
     dom = max(per, key=lambda n: per[n]["ms"])
     dom_gbs = V * per[dom]["bytes_per_voxel"] / (per[dom]["ms"] * 1e-3) / 1e9
 
@@ -1082,7 +1104,9 @@ def main():
                          "traffic_source": TRAFFIC_SOURCE,
                          "algorithmic_bytes": int(V * per[dom]["bytes_per_voxel"]),
                          **({"alu_pipe_busy": NCU_ALU_PIPE_BUSY[dom],
-                             "note": "selection network: bound by the min/max (ALU) pipe, not HBM"}
+                             "note": "selection network: bound by the min/max (ALU) pipe, not HBM",
+                             **{k: per[dom][k] for k in ("minmax_per_voxel", "alu_floor_ms", "alu_frac")
+                                if k in per[dom]}}
                             if dom in NCU_ALU_PIPE_BUSY else {})},
             "gpu_launches": launches,
             "clocks": clocks.result,
