@@ -24,7 +24,11 @@
 //  * sphere (8/16-bit): likewise the merge of planes z and z+1 (16 ranks)
 //    serves z and z+1, each adding its other plane's block and six singles;
 //    16-bit rows of whole vectors read staged planes from a ring of eight in
-//    shared memory (k_median_sphere33_st);
+//    shared memory (k_median_sphere33_st); float rows of whole vectors run
+//    the same pairs on one column per thread, with the keys computed once in
+//    shared memory (k_median_sphere33_stf);
+//  * the staged kernels alternate two register sets of sorted blocks from
+//    one z pair to the next instead of moving them;
 //  * the next z-pair's planes are loaded before the current pair's networks.
 // Borders clamp exactly as the reference's reads do.
 #include <cstdlib>
