@@ -593,10 +593,12 @@ template <class K> bool smem_ok(K kern, size_t smem) {
 // z-chunks: CLK_SEP3_CHUNKS in the environment fixes the count (tuning).
 // Otherwise about seven waves of CTAs (ctas_per_sm resident per SM), each
 // chunk long enough that its 2CZ halo planes stay a small overhead: at least
-// max(16, 24 CZ) planes while the tiles alone fill the SMs, max(8, 4 CZ) for
-// small images, where parallelism matters more (measured on 1024 x 1024 x
-// 256: minimum r5 0.47 ms with one chunk per tile, 0.29 with four to eight;
-// the Gaussian cz = 5 best with two chunks, 1.12 ms against 1.17 with three).
+// max(16, 24 CZ) planes while the tiles alone fill the SMs (measured on 1024
+// x 1024 x 256: minimum r5 0.47 ms with one chunk per tile, 0.29 with four
+// to eight; the Gaussian cz = 5 best with two chunks, 1.12 ms against 1.17
+// with three).  Small images take the count whose CTAs fill the resident
+// slots in whole waves (wave_chunks; 256x256x64 Gaussian s(2,2,1): eight
+// chunks, 0.027 ms against 0.035 with five).
 inline int chunk_count(int tiles, int depth, int cz, int ctas_per_sm) {
   static const int forced = [] {
     const char* e = getenv("CLK_SEP3_CHUNKS");
@@ -606,9 +608,11 @@ inline int chunk_count(int tiles, int depth, int cz, int ctas_per_sm) {
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (tiles < sms)  // small images: the count that fills the resident slots in whole waves
+    return wave_chunks(tiles, depth, 2 * cz, (int64_t)sms * ctas_per_sm, 1, std::max(1, depth / 4));
   const int64_t want = (int64_t)7 * sms * ctas_per_sm;
   int chunks = (int)std::max<int64_t>(1, (want + tiles / 2) / std::max(1, tiles));
-  const int minlen = tiles >= sms ? std::max(16, 24 * cz) : std::max(8, 4 * cz);
+  const int minlen = std::max(16, 24 * cz);
   chunks = std::min(chunks, std::max(1, depth / minlen));
   return chunks;
 }
