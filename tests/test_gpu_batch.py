@@ -102,6 +102,23 @@ def test_batched_tophat_matches_oracle_on_integer_images(clk, oracle, tmp_path, 
         assert np.array_equal(got[k], cur), (k, a.shape, a.dtype)
 
 
+def test_batched_medians_on_rows_of_whole_vectors_match_oracle(clk, oracle, tmp_path, monkeypatch):
+    # widths of whole 16-byte vectors take the staged bodies (float keys for
+    # f32, staged plane tiles for 16-bit pixels), the others the pair bodies
+    rng = np.random.default_rng(54)
+    imgs = []
+    for dt, w in ((np.float32, 36), (np.float32, 64), (np.float32, 38), (np.uint16, 72), (np.uint16, 66),
+                  (np.int16, 40), (np.uint8, 48)):
+        a = random_image(rng, (int(rng.integers(5, 12)), int(rng.integers(9, 40)), w), dt)
+        imgs.append(np.abs(a) if np.dtype(dt) == np.float32 else a)
+    for name, N in (("median_sphere", (5, 5, 5)), ("median_box", (3, 3, 3))):
+        got, want, _ = run_both(clk, [clk.op_kernel(name, N)], imgs, tmp_path, monkeypatch)
+        for k, a in enumerate(imgs):
+            ref = oracle.execute(name + "_3d", a, a.dtype, list(N))
+            assert got[k].tobytes() == ref.tobytes(), (name, a.shape, a.dtype)
+            assert want[k].tobytes() == ref.tobytes(), (name, a.shape, a.dtype)
+
+
 def test_one_launch_per_step_type_and_body(clk, tmp_path, monkeypatch):
     import torch
     monkeypatch.setenv("CLK_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
